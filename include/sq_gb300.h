@@ -1,0 +1,144 @@
+/*
+ * sq_gb300.h -- C ABI of the GB300 Spectral Quadrature engine.
+ *
+ * The library replaces the per-node Spectral Quadrature path of SQMiniApp:
+ * the truncated-cube Hamiltonian matvec (src/lsdft_matvec.cc), the nonlocal
+ * projector setup and apply (src/lsdft_nl.cc), the Lanczos recurrence and the
+ * tridiagonal quadrature of src/lsdft_scf.cc:32-164 and
+ * src/lsdft_tools.cc:912-1026, and the density / Fermi-level / energy closure
+ * that src/lsdft.h:98-102,209 declares.  Everything runs on one GPU; there is
+ * no CPU fallback.  All pointers are plain host or device pointers, all sizes
+ * are element counts, and every call returns an sq_status.
+ *
+ * Threading: one handle is single-threaded and stream-ordered; separate
+ * handles are independent.  The handle owns its device buffers; the caller
+ * owns every buffer it passes in.
+ */
+#ifndef SQ_GB300_H
+#define SQ_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference exit(1)s on every error (src/lsdft_readfiles.cc:141-145,
+ * :874-877; src/lsdft_tools.cc:20-26,136-139,950-952); here each one is a return value. */
+typedef enum sq_status {
+  SQ_OK = 0,
+  SQ_BAD_INPUT = 1,          /* unreadable deck, inconsistent sizes, unsupported option */
+  SQ_NO_CONVERGENCE = 2,     /* implicit QL needed more than 50 sweeps (tools.cc:950-952) */
+  SQ_LANCZOS_BREAKDOWN = 3,  /* b_k == 0: the reference divides by it (scf.cc:131,147) */
+  SQ_DEVICE_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  SQ_CUDA_ERROR = 5,         /* a CUDA runtime call failed */
+  SQ_CAPACITY = 6            /* a per-node atom list exceeded its on-chip capacity */
+} sq_status;
+
+typedef struct sq_handle sq_handle;
+
+/* Engine options. */
+typedef struct sq_options {
+  /* 1: keep the reference operator exactly, including its quirks: all (l,m) projectors of an
+   *    atom share one coefficient (src/lsdft_matvec.cc:97-100,136-138), periodic images come
+   *    from the pseudocharge cutoff (src/lsdft_initObjs.cc:1765-1772) and
+   *    BOUNDARY_CONDITION 2 adds no images (:1763-1784).
+   * 0: corrected operator: one coefficient per (atom,l,m) (src/lsdft_matvec.cc:214-227),
+   *    image range from Rcut plus the projector radius, images for every periodic BC. */
+  int faithful;
+  /* 32: FP32 Lanczos vectors and matvecs, FP64 recurrence coefficients, quadrature and sums.
+   * 64: FP64 everywhere. */
+  int precision;
+  int device;   /* CUDA device ordinal */
+} sq_options;
+
+/* Engine facts after setup. */
+typedef struct sq_info {
+  int grid[3];          /* FD nodes per axis (FD_GRID) */
+  int cube[3];          /* truncated-cube points per axis, 2*ceil(Rcut/h)+1 (readfiles.cc:442-444) */
+  int n_qp;             /* LANCZOS_DEGREE */
+  int fd_half_order;    /* FD_ORDER / 2 */
+  int bc;               /* BOUNDARY_CONDITION */
+  int n_atoms;
+  int n_types;
+  int n_images;         /* atom images whose projector box meets the extended domain */
+  int n_tables;         /* distinct projector tables after periodic deduplication */
+  int max_images_per_node;  /* on-chip capacity of the per-node image list */
+  int precision;
+  int faithful;
+  long n_nodes;         /* grid[0]*grid[1]*grid[2] */
+  double h[3];          /* mesh spacing */
+  double cell_half[3];  /* CELL: half side lengths R */
+  double rcut;
+  double beta;          /* BETA, 1/Ha */
+  double dV;
+  double n_electrons;   /* sum of valence electrons from the .ion file */
+} sq_info;
+
+/* Read <deck_dir>/<name>.inpt/.ion/.relax and <deck_dir>/pseudopotential/<psd> and build the
+ * engine.  Replaces Get_Input + Initialize + GetInfluencingAtoms_Nonlocal +
+ * CalculateNonlocalProjectors + NonlocalProjectors (src/main.cc:32-44,
+ * src/lsdft_initObjs.cc:36-93,1671-1946, src/lsdft_nl.cc:6-208). */
+sq_status sq_create_from_deck(const char *deck_dir, const char *name, const sq_options *opt,
+                              sq_handle **out);
+void sq_destroy(sq_handle *h);
+
+/* Host-only setup report (no GPU touched): parse the deck and run the host setup, then fill
+ * info (precision/device fields 0), gamma[n_types*4] (Gamma_l, 0 for the local l;
+ * src/lsdft_initObjs.cc:822-869) and cutoff[n_types*3] (pseudocharge cutoff per axis;
+ * src/lsdft_initObjs.cc:628-817).  gamma and cutoff may be NULL. */
+sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful, sq_info *info,
+                           double *gamma, double *cutoff);
+sq_status sq_get_info(const sq_handle *h, sq_info *info);
+
+/* Per-node Lanczos + Gauss quadrature for nodes [node_begin, node_end) in the reference's
+ * node order (z slowest, x fastest; src/lsdft_scf.cc:60-67).  Replaces
+ * NodesAndWeights_LSSGQ (src/lsdft.h:132, called at src/main.cc:54), which loops
+ * CalculateSpectralNodesAndWeights (src/lsdft.h:131) with Mult_NonlocalVector
+ * (src/lsdft.h:25) and TridiagEigenVecSolve_NodesAndWeights (src/lsdft.h:163-164).
+ * HOST buffers: veff[grid] (NULL = the constant veff_const on every cube point, the
+ * reference's placeholder is 0.333, src/lsdft_scf.cc:71), lambda/weights
+ * [node_end-node_begin][n_qp], lambda_min/lambda_max [node_end-node_begin].
+ * Host<->device copies happen inside the call. */
+sq_status sq_nodes_and_weights(sq_handle *h, const double *veff, double veff_const,
+                               long node_begin, long node_end, double *lambda, double *weights,
+                               double *lambda_min, double *lambda_max);
+
+/* The same on DEVICE buffers, asynchronous on `stream` (a cudaStream_t, NULL = the legacy
+ * default stream).  d_veff may be NULL (constant veff_const). */
+sq_status sq_nodes_and_weights_device(sq_handle *h, const double *d_veff, double veff_const,
+                                      long node_begin, long node_end, double *d_lambda,
+                                      double *d_weights, double *d_lambda_min,
+                                      double *d_lambda_max, void *stream);
+
+/* Wait for `stream` and report the device-side status of the preceding device calls
+ * (capacity overflow, Lanczos breakdown, QL non-convergence, device timeout). */
+sq_status sq_sync_status(sq_handle *h, void *stream);
+
+/* Copy the Lanczos coefficients a_k, b_k (k < n_qp) of the last nodes_and_weights call to
+ * host arrays [n][n_qp] (the lssgq recurrence of src/lsdft_scf.cc:111-150). */
+sq_status sq_copy_lanczos_coefficients(sq_handle *h, double *a, double *b, long n);
+
+/* Fermi level by bisection, node densities and band energy (FP64), from the quadrature of
+ * the nodes: N_e(lf) = 2 sum_nodes sum_q w f(lambda - lf), rho = (2/dV) sum_q w f,
+ * e_band = 2 sum w lambda f, ts = (2/beta) sum w [f ln f + (1-f) ln(1-f)].
+ * Implements the API that src/lsdft.h:98-102,209 declares (constraint_lssgq, FermiDirac,
+ * CalculateDensity_lssgq, findRootBrent, SystemEnergy_Calc_lssgq) but never defines.
+ * HOST buffers: lambda, weights [n_nodes][n_qp]; rho [n_nodes] (may be NULL). */
+sq_status sq_fermi_density_energy(sq_handle *h, const double *lambda, const double *weights,
+                                  long n_nodes, double n_electrons, double tol,
+                                  double *lambda_f, double *rho, double *e_band, double *ts);
+
+/* The same on DEVICE buffers (d_rho may be NULL); scalars are returned to host memory.
+ * Synchronises `stream` before returning. */
+sq_status sq_fermi_density_energy_device(sq_handle *h, const double *d_lambda,
+                                         const double *d_weights, long n_nodes,
+                                         double n_electrons, double tol, double *lambda_f,
+                                         double *d_rho, double *e_band, double *ts,
+                                         void *stream);
+
+/* Message of the last failing call on this thread. */
+const char *sq_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

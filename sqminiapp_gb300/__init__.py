@@ -1,0 +1,152 @@
+"""GB300 Spectral Quadrature engine: Python mirror of the reference's per-node SQ API.
+
+The compute path is the in-tree CUDA library ``lib/libsq_gb300.so`` (sm_103a) behind the
+C ABI of ``include/sq_gb300.h``; this module only binds it with ctypes.  There is no CPU
+fallback: if the library is missing the import of :class:`LSDFT` fails loudly.
+
+Names follow the reference (SQMiniApp ``src/lsdft.h``):
+
+* ``LSDFT(deck_dir, name)``         -- Get_Input + Initialize + GetInfluencingAtoms_Nonlocal +
+                                       CalculateNonlocalProjectors + NonlocalProjectors
+                                       (src/main.cc:32-44)
+* ``LSDFT.NodesAndWeights_LSSGQ``   -- src/lsdft_scf.cc:32-82 (per-node Lanczos + quadrature)
+* ``LSDFT.CalculateDensity_lssgq``  -- declared at src/lsdft.h:100 (Fermi bisection, density,
+                                       band energy), implemented from the SQ method
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .capi import SQ_OK, SqError, SqInfo, SqOptions, lib, check, library_path
+
+__all__ = ["LSDFT", "SqError", "library_path", "DECK_DIR"]
+
+DECK_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "decks")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class LSDFT:
+    """One SQ engine on one GPU, built from a reference input deck.
+
+    faithful=True keeps the reference operator with its quirks (shared projector
+    coefficient per atom, pseudocharge-based image range); faithful=False (default) is the
+    corrected operator.  precision=32 runs FP32 Lanczos vectors with FP64 recurrence
+    coefficients, quadrature and sums; precision=64 is FP64 throughout.
+    """
+
+    def __init__(self, deck_dir, name, faithful=False, precision=32, device=0):
+        self._lib = lib()
+        self._h = ctypes.c_void_p()
+        opt = SqOptions(int(bool(faithful)), int(precision), int(device))
+        check(self._lib.sq_create_from_deck(deck_dir.encode(), name.encode(), ctypes.byref(opt),
+                                            ctypes.byref(self._h)), "sq_create_from_deck")
+        info = SqInfo()
+        check(self._lib.sq_get_info(self._h, ctypes.byref(info)), "sq_get_info")
+        self.info = info
+        self.grid = tuple(info.grid)
+        self.cube = tuple(info.cube)
+        self.n_qp = info.n_qp
+        self.n_nodes = info.n_nodes
+        self.h = tuple(info.h)
+        self.dV = info.dV
+        self.beta = info.beta
+        self.n_electrons = info.n_electrons
+        self.precision = precision
+        self.faithful = bool(faithful)
+
+    def close(self):
+        if self._h:
+            self._lib.sq_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # --- per-node Lanczos + Gauss quadrature -------------------------------------------
+    def NodesAndWeights_LSSGQ(self, veff=None, veff_const=0.333, node_begin=0, node_end=None):
+        """Quadrature nodes/weights of nodes [node_begin, node_end) (host arrays).
+
+        veff: None for a constant ``veff_const`` (the reference's placeholder is 0.333,
+        src/lsdft_scf.cc:71) or an array over the FD grid (z slowest, x fastest)."""
+        if node_end is None:
+            node_end = self.n_nodes
+        n = node_end - node_begin
+        lam = np.empty((n, self.n_qp))
+        w = np.empty((n, self.n_qp))
+        lmin = np.empty(n)
+        lmax = np.empty(n)
+        vp = None
+        if veff is not None:
+            veff = np.ascontiguousarray(veff, dtype=np.float64).reshape(-1)
+            if veff.size != self.n_nodes:
+                raise ValueError("veff must have one value per FD node")
+            vp = _ptr(veff)
+        check(self._lib.sq_nodes_and_weights(self._h, vp, float(veff_const), int(node_begin),
+                                             int(node_end), _ptr(lam), _ptr(w), _ptr(lmin),
+                                             _ptr(lmax)), "sq_nodes_and_weights")
+        return {"lambda": lam, "weights": w, "lambda_min": lmin, "lambda_max": lmax}
+
+    def nodes_and_weights_device(self, d_veff, veff_const, node_begin, node_end, d_lambda,
+                                 d_weights, d_lmin, d_lmax, stream=0):
+        """Asynchronous device-pointer form (integers are raw CUDA device addresses)."""
+        check(self._lib.sq_nodes_and_weights_device(
+            self._h, ctypes.c_void_p(d_veff) if d_veff else None, float(veff_const),
+            int(node_begin), int(node_end), ctypes.c_void_p(d_lambda), ctypes.c_void_p(d_weights),
+            ctypes.c_void_p(d_lmin), ctypes.c_void_p(d_lmax), ctypes.c_void_p(stream)),
+            "sq_nodes_and_weights_device")
+
+    def sync_status(self, stream=0):
+        check(self._lib.sq_sync_status(self._h, ctypes.c_void_p(stream)), "sq_sync_status")
+
+    def lanczos_coefficients(self, n):
+        """a_k, b_k (k < n_qp) of the first n nodes of the last call."""
+        a = np.empty((n, self.n_qp))
+        b = np.empty((n, self.n_qp))
+        check(self._lib.sq_copy_lanczos_coefficients(self._h, _ptr(a), _ptr(b), int(n)),
+              "sq_copy_lanczos_coefficients")
+        return a, b
+
+    # --- Fermi level, density, energy ----------------------------------------------------
+    def CalculateDensity_lssgq(self, lam, weights, n_electrons=None, tol=1e-12):
+        """Fermi level by bisection, node densities, band energy and -TS (FP64)."""
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        weights = np.ascontiguousarray(weights, dtype=np.float64)
+        n_nodes = lam.shape[0]
+        if n_electrons is None:
+            n_electrons = self.n_electrons
+        rho = np.empty(n_nodes)
+        lf = ctypes.c_double()
+        eb = ctypes.c_double()
+        ts = ctypes.c_double()
+        check(self._lib.sq_fermi_density_energy(self._h, _ptr(lam), _ptr(weights), n_nodes,
+                                                float(n_electrons), float(tol), ctypes.byref(lf),
+                                                _ptr(rho), ctypes.byref(eb), ctypes.byref(ts)),
+              "sq_fermi_density_energy")
+        return {"lambda_f": lf.value, "rho": rho, "e_band": eb.value, "ts": ts.value}
+
+    def fermi_density_energy_device(self, d_lambda, d_weights, n_nodes, n_electrons, tol,
+                                    d_rho, stream=0):
+        lf = ctypes.c_double()
+        eb = ctypes.c_double()
+        ts = ctypes.c_double()
+        check(self._lib.sq_fermi_density_energy_device(
+            self._h, ctypes.c_void_p(d_lambda), ctypes.c_void_p(d_weights), int(n_nodes),
+            float(n_electrons), float(tol), ctypes.byref(lf),
+            ctypes.c_void_p(d_rho) if d_rho else None, ctypes.byref(eb), ctypes.byref(ts),
+            ctypes.c_void_p(stream)), "sq_fermi_density_energy_device")
+        return {"lambda_f": lf.value, "e_band": eb.value, "ts": ts.value}

@@ -1,0 +1,82 @@
+"""ctypes declarations of include/sq_gb300.h for the in-tree library lib/libsq_gb300.so."""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(HERE, "lib", "libsq_gb300.so")
+
+SQ_OK = 0
+STATUS_NAMES = {0: "SQ_OK", 1: "SQ_BAD_INPUT", 2: "SQ_NO_CONVERGENCE", 3: "SQ_LANCZOS_BREAKDOWN",
+                4: "SQ_DEVICE_TIMEOUT", 5: "SQ_CUDA_ERROR", 6: "SQ_CAPACITY"}
+
+# every function the header declares, with its ctypes signature
+_dp = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+_l = ctypes.c_long
+_d = ctypes.c_double
+
+
+class SqOptions(ctypes.Structure):
+    _fields_ = [("faithful", ctypes.c_int), ("precision", ctypes.c_int), ("device", ctypes.c_int)]
+
+
+class SqInfo(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_int * 3), ("cube", ctypes.c_int * 3), ("n_qp", ctypes.c_int),
+                ("fd_half_order", ctypes.c_int), ("bc", ctypes.c_int), ("n_atoms", ctypes.c_int),
+                ("n_types", ctypes.c_int), ("n_images", ctypes.c_int),
+                ("n_tables", ctypes.c_int), ("max_images_per_node", ctypes.c_int),
+                ("precision", ctypes.c_int), ("faithful", ctypes.c_int), ("n_nodes", ctypes.c_long),
+                ("h", ctypes.c_double * 3), ("cell_half", ctypes.c_double * 3),
+                ("rcut", ctypes.c_double), ("beta", ctypes.c_double), ("dV", ctypes.c_double),
+                ("n_electrons", ctypes.c_double)]
+
+
+SIGNATURES = {
+    "sq_create_from_deck": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p,
+                                           ctypes.POINTER(SqOptions), ctypes.POINTER(_vp)]),
+    "sq_destroy": (None, [_vp]),
+    "sq_describe_deck": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                        ctypes.POINTER(SqInfo), _dp, _dp]),
+    "sq_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(SqInfo)]),
+    "sq_nodes_and_weights": (ctypes.c_int, [_vp, _dp, _d, _l, _l, _dp, _dp, _dp, _dp]),
+    "sq_nodes_and_weights_device": (ctypes.c_int, [_vp, _vp, _d, _l, _l, _vp, _vp, _vp, _vp, _vp]),
+    "sq_sync_status": (ctypes.c_int, [_vp, _vp]),
+    "sq_copy_lanczos_coefficients": (ctypes.c_int, [_vp, _dp, _dp, _l]),
+    "sq_fermi_density_energy": (ctypes.c_int, [_vp, _dp, _dp, _l, _d, _d, _dp, _dp, _dp, _dp]),
+    "sq_fermi_density_energy_device": (ctypes.c_int, [_vp, _vp, _vp, _l, _d, _d, _dp, _vp, _dp,
+                                                      _dp, _vp]),
+    "sq_last_error_string": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+class SqError(RuntimeError):
+    def __init__(self, status, where, msg):
+        super().__init__("%s failed: %s (%s)" % (where, STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def library_path():
+    return _LIB
+
+
+def lib():
+    """Load the CUDA library; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            raise ImportError("sqminiapp_gb300 native library missing (%s); run "
+                              "`python -c 'import __graft_entry__ as g; g.build()'`" % _LIB)
+        L = ctypes.CDLL(_LIB)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, where):
+    if status != SQ_OK:
+        raise SqError(status, where, lib().sq_last_error_string().decode())

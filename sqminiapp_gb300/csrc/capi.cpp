@@ -1,0 +1,507 @@
+// capi.cpp -- the C ABI of include/sq_gb300.h.
+//
+// A handle owns the parsed deck, the host setup and the device buffers.  Every entry point
+// returns sq_status; fatal paths of the reference (exit(1)) become SQ_BAD_INPUT,
+// SQ_NO_CONVERGENCE, ... and sq_last_error_string() gives the message.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/sq_gb300.h"
+#include "sq_internal.hpp"
+#include "sq_kernels.hpp"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+sq_status fail(sq_status s, const std::string &msg) {
+  g_last_error = msg;
+  return s;
+}
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string &m) : std::runtime_error(m) {}
+};
+
+void ck(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <typename P> void dev_alloc(P **ptr, size_t bytes, const char *what) {
+  *ptr = nullptr;
+  if (bytes == 0) bytes = 16;
+  ck(cudaMalloc((void **)ptr, bytes), what);
+}
+
+template <typename P> void dev_free(P *&ptr) {
+  if (ptr) cudaFree((void *)ptr);
+  ptr = nullptr;
+}
+
+}  // namespace
+
+struct sq_handle {
+  sq::Deck deck;
+  sq::Setup setup;
+  sq_options opt{};
+  sq_info info{};
+  sq::LanczosParams lp{};
+  int num_sms = 0;
+  bool u_smem = false;
+  size_t smem = 0;
+  int grid = 0;
+  int fermi_grid = 0;
+  size_t elem = 4;
+  // device buffers owned by the handle
+  sq::ImageMeta *d_images = nullptr;
+  void *d_tables = nullptr;
+  void *d_veff_ext = nullptr;
+  double *d_veff_in = nullptr;
+  void *d_u = nullptr;
+  int *d_status = nullptr;
+  double *d_ab = nullptr;
+  long long ab_cap = 0;
+  long long last_n = 0;
+  double *d_lambda = nullptr, *d_w = nullptr, *d_lmin = nullptr, *d_lmax = nullptr;
+  long long out_cap = 0;
+  double *d_rho = nullptr;
+  long long rho_cap = 0;
+  double *d_fermi_scratch = nullptr;
+  unsigned *d_bar = nullptr;
+  double *d_fermi_out = nullptr;
+  int fermi_maxit = 400;
+  cudaStream_t own_stream = nullptr;
+
+  ~sq_handle() {
+    dev_free(d_images);
+    dev_free(d_tables);
+    dev_free(d_veff_ext);
+    dev_free(d_veff_in);
+    dev_free(d_u);
+    dev_free(d_status);
+    dev_free(d_ab);
+    dev_free(d_lambda);
+    dev_free(d_w);
+    dev_free(d_lmin);
+    dev_free(d_lmax);
+    dev_free(d_rho);
+    dev_free(d_fermi_scratch);
+    dev_free(d_bar);
+    dev_free(d_fermi_out);
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+};
+
+namespace {
+
+// Largest number of images that meet one node's cube, by a 3D difference array over the
+// node grid: image box [b, b+f) meets the cube of node I iff I in [b - nh, b + f - 1 + nh].
+int max_images_per_node(const sq::Setup &s, const sq::Deck &d) {
+  const int N[3] = {d.grid[0], d.grid[1], d.grid[2]};
+  const int M[3] = {N[0] + 1, N[1] + 1, N[2] + 1};
+  std::vector<int> diff((size_t)M[0] * M[1] * M[2], 0);
+  auto at = [&](int x, int y, int z) -> int & { return diff[((size_t)z * M[1] + y) * M[0] + x]; };
+  for (const sq::ImageMeta &im : s.images) {
+    const sq::TypeDesc &td = s.types[im.type];
+    const int b[3] = {im.bx, im.by, im.bz}, f[3] = {td.fx, td.fy, td.fz};
+    int lo[3], hi[3];
+    bool empty = false;
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::max(0, b[a] - s.nh[a]);
+      hi[a] = std::min(N[a] - 1, b[a] + f[a] - 1 + s.nh[a]);
+      if (lo[a] > hi[a]) empty = true;
+    }
+    if (empty) continue;
+    for (int c = 0; c < 8; c++) {
+      const int x = (c & 1) ? hi[0] + 1 : lo[0];
+      const int y = (c & 2) ? hi[1] + 1 : lo[1];
+      const int z = (c & 4) ? hi[2] + 1 : lo[2];
+      at(x, y, z) += (__builtin_popcount(c) & 1) ? -1 : 1;
+    }
+  }
+  int best = 0;
+  for (int z = 0; z < M[2]; z++)
+    for (int y = 0; y < M[1]; y++)
+      for (int x = 0; x < M[0]; x++) {
+        int v = at(x, y, z);
+        if (x > 0) v += at(x - 1, y, z);
+        if (y > 0) v += at(x, y - 1, z);
+        if (z > 0) v += at(x, y, z - 1);
+        if (x > 0 && y > 0) v -= at(x - 1, y - 1, z);
+        if (x > 0 && z > 0) v -= at(x - 1, y, z - 1);
+        if (y > 0 && z > 0) v -= at(x, y - 1, z - 1);
+        if (x > 0 && y > 0 && z > 0) v += at(x - 1, y - 1, z - 1);
+        at(x, y, z) = v;
+        if (x < N[0] && y < N[1] && z < N[2]) best = std::max(best, v);
+      }
+  return best;
+}
+
+void ensure_capacity(double *&ptr, long long &cap, long long need, const char *what) {
+  if (need <= cap) return;
+  dev_free(ptr);
+  dev_alloc(&ptr, sizeof(double) * (size_t)need, what);
+  cap = need;
+}
+
+void fill_info(sq_info &in, const sq::Deck &d, const sq::Setup &s, int max_img,
+               const sq_options &opt) {
+  for (int a = 0; a < 3; a++) {
+    in.grid[a] = d.grid[a];
+    in.cube[a] = s.cube[a];
+    in.h[a] = s.h[a];
+    in.cell_half[a] = d.cell_half[a];
+  }
+  in.n_qp = d.n_qp;
+  in.fd_half_order = d.half_order;
+  in.bc = d.bc;
+  in.n_atoms = (int)d.atom_type.size();
+  in.n_types = (int)d.psd.size();
+  in.n_images = (int)s.images.size();
+  in.n_tables = s.n_tables;
+  in.max_images_per_node = max_img;
+  in.precision = opt.precision;
+  in.faithful = opt.faithful;
+  in.n_nodes = (long)d.grid[0] * d.grid[1] * d.grid[2];
+  in.rcut = d.rcut;
+  in.beta = d.beta;
+  in.dV = s.dV;
+  in.n_electrons = d.n_electrons;
+}
+
+void build_engine(sq_handle *h) {
+  const sq::Deck &d = h->deck;
+  const sq::Setup &s = h->setup;
+  ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+  ck(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->opt.device), "sm count");
+  int smem_optin = 0;
+  ck(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->opt.device),
+     "smem optin");
+  ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
+
+  sq::LanczosParams &p = h->lp;
+  p.nx = s.cube[0];
+  p.ny = s.cube[1];
+  p.nz = s.cube[2];
+  p.nhx = s.nh[0];
+  p.nhy = s.nh[1];
+  p.nhz = s.nh[2];
+  p.Nx = d.grid[0];
+  p.Ny = d.grid[1];
+  p.Nz = d.grid[2];
+  p.EX = p.Nx + 2 * p.nhx;
+  p.EY = p.Ny + 2 * p.nhy;
+  p.EZ = p.Nz + 2 * p.nhz;
+  p.pitch = p.nx + sq::kStencilHalf;
+  p.nqp = d.n_qp;
+  p.n_images = (int)s.images.size();
+  p.ntype = (int)s.types.size();
+  p.hx = s.h[0];
+  p.hy = s.h[1];
+  p.hz = s.h[2];
+  p.cdiag = s.c[0][0] + s.c[1][0] + s.c[2][0];
+  p.cdiagf = (float)p.cdiag;
+  for (int q = 0; q <= sq::kStencilHalf; q++) {
+    p.cx[q] = s.c[0][q];
+    p.cy[q] = s.c[1][q];
+    p.cz[q] = s.c[2][q];
+    p.cxf[q] = (float)p.cx[q];
+    p.cyf[q] = (float)p.cy[q];
+    p.czf[q] = (float)p.cz[q];
+  }
+  p.union_mask = 0;
+  for (size_t t = 0; t < s.types.size(); t++) {
+    p.types[t] = s.types[t];
+    p.union_mask |= s.types[t].chan_mask;
+  }
+  int rank = 0;
+  for (int l = 0; l < 4; l++)
+    for (int m = -l; m <= l; m++) p.lm_rank[l * l + l + m] = (p.union_mask & (1 << l)) ? rank++ : -1;
+  p.alpha_stride = h->opt.faithful ? 1 : std::max(rank, 1);
+
+  if (p.nx > 32) throw std::invalid_argument("cubes wider than 32 points in x are not supported");
+  if (d.n_qp > 64) throw std::invalid_argument("LANCZOS_DEGREE above 64 is not supported");
+
+  const int need_img = std::max(1, max_images_per_node(s, d));
+  p.max_img = need_img;
+  h->elem = h->opt.precision == 32 ? 4 : 8;
+  const int block = h->opt.precision == 32 ? sq::kBlockF32 : sq::kBlockF64;
+  h->u_smem = false;
+  if (h->opt.precision == 32 &&
+      sq::lanczos_smem_bytes(p, 4, true, block) <= (size_t)smem_optin)
+    h->u_smem = true;
+  h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, block);
+  if (h->smem > (size_t)smem_optin)
+    throw std::invalid_argument("cube of " + std::to_string(p.nx) + "x" + std::to_string(p.ny) +
+                                "x" + std::to_string(p.nz) +
+                                " does not fit in shared memory at this precision");
+  h->grid = h->num_sms;
+
+  // device buffers
+  dev_alloc(&h->d_images, sizeof(sq::ImageMeta) * s.images.size(), "images");
+  ck(cudaMemcpy(h->d_images, s.images.data(), sizeof(sq::ImageMeta) * s.images.size(),
+                cudaMemcpyHostToDevice), "images H2D");
+  dev_alloc(&h->d_tables, h->elem * s.tables.size(), "tables");
+  if (h->opt.precision == 32) {
+    std::vector<float> t32(s.tables.begin(), s.tables.end());
+    ck(cudaMemcpy(h->d_tables, t32.data(), 4 * t32.size(), cudaMemcpyHostToDevice), "tables H2D");
+  } else {
+    ck(cudaMemcpy(h->d_tables, s.tables.data(), 8 * s.tables.size(), cudaMemcpyHostToDevice),
+       "tables H2D");
+  }
+  dev_alloc(&h->d_veff_ext, h->elem * (size_t)p.EX * p.EY * p.EZ, "veff_ext");
+  dev_alloc(&h->d_veff_in, sizeof(double) * (size_t)p.Nx * p.Ny * p.Nz, "veff");
+  if (!h->u_smem) {
+    const size_t nc4 = ((size_t)p.nx * p.ny * p.nz + 3) & ~size_t(3);
+    dev_alloc(&h->d_u, h->elem * nc4 * h->grid, "U scratch");
+  }
+  dev_alloc(&h->d_status, sizeof(int) * 4, "status");
+  ck(cudaMemset(h->d_status, 0, sizeof(int) * 4), "status memset");
+  h->fermi_grid = h->num_sms;
+  dev_alloc(&h->d_fermi_scratch, sizeof(double) * sq::fermi_scratch_doubles(h->fermi_grid, h->fermi_maxit),
+            "fermi scratch");
+  dev_alloc(&h->d_bar, sizeof(unsigned) * 2, "barrier");
+  dev_alloc(&h->d_fermi_out, sizeof(double) * 4, "fermi out");
+
+  fill_info(h->info, d, s, p.max_img, h->opt);
+}
+
+sq_status device_status(sq_handle *h, cudaStream_t s) {
+  int st = 0;
+  ck(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, s), "status D2H");
+  ck(cudaStreamSynchronize(s), "sync");
+  if (st & sq::kStatusTimeout) return fail(SQ_DEVICE_TIMEOUT, "a device-side wait gave up");
+  if (st & sq::kStatusCapacity) return fail(SQ_CAPACITY, "per-node image list overflow");
+  if (st & sq::kStatusNoConvergence)
+    return fail(SQ_NO_CONVERGENCE, "Too many iterations in Tridiagonal solver");
+  if (st & sq::kStatusBreakdown) return fail(SQ_LANCZOS_BREAKDOWN, "Lanczos breakdown (b_k == 0)");
+  return SQ_OK;
+}
+
+sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long long nb,
+                     long long ne, double *d_lambda, double *d_w, double *d_lmin, double *d_lmax,
+                     cudaStream_t s) {
+  const long long n = ne - nb;
+  if (nb < 0 || ne > h->info.n_nodes || n <= 0)
+    return fail(SQ_BAD_INPUT, "node range outside the grid");
+  ensure_capacity(h->d_ab, h->ab_cap, 2 * (long long)h->lp.nqp * n, "lanczos coefficients");
+  sq::LanczosParams p = h->lp;
+  p.node_begin = nb;
+  p.node_end = ne;
+  ck(cudaMemsetAsync(h->d_status, 0, sizeof(int), s), "status reset");
+  ck(sq::launch_veff_extend(d_veff, veff_const, h->d_veff_ext, h->opt.precision, p, s), "veff");
+  const int grid = (int)std::min<long long>(h->grid, n);
+  ck(sq::launch_lanczos(p, h->opt.precision, h->opt.faithful != 0, h->u_smem, grid, h->smem, s,
+                        h->d_veff_ext, h->d_images, h->d_tables, h->d_u, h->d_ab, h->d_status),
+     "lanczos");
+  ck(sq::launch_quadrature(h->d_ab, n, p.nqp, d_lambda, d_w, d_lmin, d_lmax, h->d_status, s),
+     "quadrature");
+  h->last_n = n;
+  return SQ_OK;
+}
+
+template <typename F> sq_status guarded(F &&f) {
+  try {
+    return f();
+  } catch (const CudaError &e) {
+    return fail(SQ_CUDA_ERROR, e.what());
+  } catch (const std::exception &e) {
+    return fail(SQ_BAD_INPUT, e.what());
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+sq_status sq_create_from_deck(const char *deck_dir, const char *name, const sq_options *opt,
+                              sq_handle **out) {
+  if (!out || !deck_dir || !name) return fail(SQ_BAD_INPUT, "null argument");
+  *out = nullptr;
+  sq_handle *h = new sq_handle();
+  sq_status st = guarded([&] {
+    h->opt = opt ? *opt : sq_options{0, 32, 0};
+    if (h->opt.precision != 32 && h->opt.precision != 64)
+      return fail(SQ_BAD_INPUT, "precision must be 32 or 64");
+    h->deck = sq::read_deck(deck_dir, name);
+    h->setup = sq::build_setup(h->deck, h->opt.faithful != 0);
+    build_engine(h);
+    return SQ_OK;
+  });
+  if (st != SQ_OK) {
+    delete h;
+    return st;
+  }
+  *out = h;
+  return SQ_OK;
+}
+
+void sq_destroy(sq_handle *h) { delete h; }
+
+sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful, sq_info *info,
+                           double *gamma, double *cutoff) {
+  if (!deck_dir || !name || !info) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    sq::Deck d = sq::read_deck(deck_dir, name);
+    sq::Setup s = sq::build_setup(d, faithful != 0);
+    sq_options opt{faithful, 0, 0};
+    *info = sq_info{};
+    fill_info(*info, d, s, max_images_per_node(s, d), opt);
+    for (size_t t = 0; t < s.types.size(); t++) {
+      if (gamma)
+        for (int l = 0; l < 4; l++) gamma[4 * t + l] = s.types[t].gamma[l];
+      if (cutoff)
+        for (int a = 0; a < 3; a++) cutoff[3 * t + a] = s.pseudocharge_cutoff[3 * t + a];
+    }
+    return SQ_OK;
+  });
+}
+
+sq_status sq_get_info(const sq_handle *h, sq_info *info) {
+  if (!h || !info) return fail(SQ_BAD_INPUT, "null argument");
+  *info = h->info;
+  return SQ_OK;
+}
+
+sq_status sq_nodes_and_weights_device(sq_handle *h, const double *d_veff, double veff_const,
+                                      long node_begin, long node_end, double *d_lambda,
+                                      double *d_weights, double *d_lambda_min,
+                                      double *d_lambda_max, void *stream) {
+  if (!h || !d_lambda || !d_weights || !d_lambda_min || !d_lambda_max)
+    return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    return run_device(h, d_veff, veff_const, node_begin, node_end, d_lambda, d_weights,
+                      d_lambda_min, d_lambda_max, (cudaStream_t)stream);
+  });
+}
+
+sq_status sq_sync_status(sq_handle *h, void *stream) {
+  if (!h) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] { return device_status(h, (cudaStream_t)stream); });
+}
+
+sq_status sq_nodes_and_weights(sq_handle *h, const double *veff, double veff_const,
+                               long node_begin, long node_end, double *lambda, double *weights,
+                               double *lambda_min, double *lambda_max) {
+  if (!h || !lambda || !weights || !lambda_min || !lambda_max)
+    return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t s = h->own_stream;
+    const long long n = (long long)node_end - node_begin;
+    if (n <= 0 || node_begin < 0 || node_end > h->info.n_nodes)
+      return fail(SQ_BAD_INPUT, "node range outside the grid");
+    const long long q = h->lp.nqp;
+    long long cap = h->out_cap;
+    ensure_capacity(h->d_lambda, cap, n * q, "lambda");
+    cap = h->out_cap;
+    ensure_capacity(h->d_w, cap, n * q, "weights");
+    cap = h->out_cap;
+    ensure_capacity(h->d_lmin, cap, std::max(n * q, n), "lambda_min");
+    cap = h->out_cap;
+    ensure_capacity(h->d_lmax, cap, std::max(n * q, n), "lambda_max");
+    h->out_cap = std::max(h->out_cap, n * q);
+    const double *dv = nullptr;
+    if (veff) {
+      ck(cudaMemcpyAsync(h->d_veff_in, veff, sizeof(double) * h->info.n_nodes,
+                         cudaMemcpyHostToDevice, s), "veff H2D");
+      dv = h->d_veff_in;
+    }
+    sq_status st = run_device(h, dv, veff_const, node_begin, node_end, h->d_lambda, h->d_w,
+                              h->d_lmin, h->d_lmax, s);
+    if (st != SQ_OK) return st;
+    ck(cudaMemcpyAsync(lambda, h->d_lambda, sizeof(double) * n * q, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaMemcpyAsync(weights, h->d_w, sizeof(double) * n * q, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaMemcpyAsync(lambda_min, h->d_lmin, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaMemcpyAsync(lambda_max, h->d_lmax, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "D2H");
+    return device_status(h, s);
+  });
+}
+
+sq_status sq_copy_lanczos_coefficients(sq_handle *h, double *a, double *b, long n) {
+  if (!h || !a || !b) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    if (n > h->last_n) return fail(SQ_BAD_INPUT, "more nodes requested than the last call computed");
+    const int q = h->lp.nqp;
+    std::vector<double> ab((size_t)2 * q * n);
+    ck(cudaStreamSynchronize(h->own_stream), "sync");
+    ck(cudaDeviceSynchronize(), "sync");
+    ck(cudaMemcpy(ab.data(), h->d_ab, sizeof(double) * ab.size(), cudaMemcpyDeviceToHost), "ab D2H");
+    for (long i = 0; i < n; i++)
+      for (int k = 0; k < q; k++) {
+        a[i * q + k] = ab[(size_t)i * 2 * q + k];
+        b[i * q + k] = ab[(size_t)i * 2 * q + q + k];
+      }
+    return SQ_OK;
+  });
+}
+
+sq_status sq_fermi_density_energy_device(sq_handle *h, const double *d_lambda,
+                                         const double *d_weights, long n_nodes,
+                                         double n_electrons, double tol, double *lambda_f,
+                                         double *d_rho, double *e_band, double *ts,
+                                         void *stream) {
+  if (!h || !d_lambda || !d_weights || !lambda_f || !e_band || !ts)
+    return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    if (n_nodes <= 0) return fail(SQ_BAD_INPUT, "n_nodes must be positive");
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    ck(cudaMemsetAsync(h->d_status, 0, sizeof(int), s), "status reset");
+    ck(sq::launch_fermi(d_lambda, d_weights, n_nodes, h->lp.nqp, h->info.beta, n_electrons,
+                        h->info.dV, tol, h->fermi_maxit, d_rho, h->d_fermi_out,
+                        h->d_fermi_scratch, h->d_bar, h->d_status, h->fermi_grid, s),
+       "fermi");
+    double outv[4];
+    ck(cudaMemcpyAsync(outv, h->d_fermi_out, sizeof(outv), cudaMemcpyDeviceToHost, s), "D2H");
+    sq_status st = device_status(h, s);
+    if (st != SQ_OK) return st;
+    *lambda_f = outv[0];
+    *e_band = outv[1];
+    *ts = outv[2];
+    return SQ_OK;
+  });
+}
+
+sq_status sq_fermi_density_energy(sq_handle *h, const double *lambda, const double *weights,
+                                  long n_nodes, double n_electrons, double tol, double *lambda_f,
+                                  double *rho, double *e_band, double *ts) {
+  if (!h || !lambda || !weights || !lambda_f || !e_band || !ts)
+    return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    if (n_nodes <= 0) return fail(SQ_BAD_INPUT, "n_nodes must be positive");
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t s = h->own_stream;
+    const long long nq = (long long)n_nodes * h->lp.nqp;
+    long long cap = h->out_cap;
+    ensure_capacity(h->d_lambda, cap, nq, "lambda");
+    cap = h->out_cap;
+    ensure_capacity(h->d_w, cap, nq, "weights");
+    cap = h->out_cap;
+    ensure_capacity(h->d_lmin, cap, nq, "lambda_min");
+    cap = h->out_cap;
+    ensure_capacity(h->d_lmax, cap, nq, "lambda_max");
+    h->out_cap = std::max(h->out_cap, nq);
+    ensure_capacity(h->d_rho, h->rho_cap, n_nodes, "rho");
+    ck(cudaMemcpyAsync(h->d_lambda, lambda, sizeof(double) * nq, cudaMemcpyHostToDevice, s), "H2D");
+    ck(cudaMemcpyAsync(h->d_w, weights, sizeof(double) * nq, cudaMemcpyHostToDevice, s), "H2D");
+    sq_status st = sq_fermi_density_energy_device(h, h->d_lambda, h->d_w, n_nodes, n_electrons,
+                                                  tol, lambda_f, h->d_rho, e_band, ts, s);
+    if (st != SQ_OK) return st;
+    if (rho) {
+      ck(cudaMemcpyAsync(rho, h->d_rho, sizeof(double) * n_nodes, cudaMemcpyDeviceToHost, s), "D2H");
+      ck(cudaStreamSynchronize(s), "sync");
+    }
+    return SQ_OK;
+  });
+}
+
+const char *sq_last_error_string(void) { return g_last_error.c_str(); }
+
+}  // extern "C"
