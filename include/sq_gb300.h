@@ -71,6 +71,8 @@ typedef struct sq_info {
   double beta;          /* BETA, 1/Ha */
   double dV;
   double n_electrons;   /* sum of valence electrons from the .ion file */
+  int n_lm;             /* nonlocal (l,m) projectors per atom (union over types) */
+  double proj_points_per_node;  /* mean over nodes of sum_images |projector box ∩ cube| */
 } sq_info;
 
 /* Read <deck_dir>/<name>.inpt/.ion/.relax and <deck_dir>/pseudopotential/<psd> and build the
@@ -134,6 +136,14 @@ sq_status sq_fermi_density_energy_device(sq_handle *h, const double *d_lambda,
                                          double n_electrons, double tol, double *lambda_f,
                                          double *d_rho, double *e_band, double *ts,
                                          void *stream);
+
+/* Device time (ms) of the kernels of the last nodes_and_weights call, measured with CUDA
+ * events on the stream they ran on: ms[0] Lanczos kernel, ms[1] quadrature kernel. */
+sq_status sq_last_kernel_times(sq_handle *h, double *ms);
+
+/* Measure the FP32 FMA throughput of the device (TFLOP/s) with a register-resident FMA
+ * chain on every SM; the peak against which the FP32 Lanczos kernel is reported. */
+sq_status sq_measure_fp32_peak(int device, double *tflops);
 
 /* Message of the last failing call on this thread. */
 const char *sq_last_error_string(void);

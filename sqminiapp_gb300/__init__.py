@@ -78,18 +78,27 @@ class LSDFT:
         self.close()
 
     # --- per-node Lanczos + Gauss quadrature -------------------------------------------
-    def NodesAndWeights_LSSGQ(self, veff=None, veff_const=0.333, node_begin=0, node_end=None):
+    def NodesAndWeights_LSSGQ(self, veff=None, veff_const=0.333, node_begin=0, node_end=None,
+                              out=None):
         """Quadrature nodes/weights of nodes [node_begin, node_end) (host arrays).
 
         veff: None for a constant ``veff_const`` (the reference's placeholder is 0.333,
-        src/lsdft_scf.cc:71) or an array over the FD grid (z slowest, x fastest)."""
+        src/lsdft_scf.cc:71) or an array over the FD grid (z slowest, x fastest).
+        out: optional dict of preallocated float64 arrays (e.g. pinned memory) with keys
+        lambda, weights [n, n_qp] and lambda_min, lambda_max [n]."""
         if node_end is None:
             node_end = self.n_nodes
         n = node_end - node_begin
-        lam = np.empty((n, self.n_qp))
-        w = np.empty((n, self.n_qp))
-        lmin = np.empty(n)
-        lmax = np.empty(n)
+        if out is None:
+            lam = np.empty((n, self.n_qp))
+            w = np.empty((n, self.n_qp))
+            lmin = np.empty(n)
+            lmax = np.empty(n)
+        else:
+            lam, w, lmin, lmax = out["lambda"], out["weights"], out["lambda_min"], out["lambda_max"]
+            for a, shape in ((lam, (n, self.n_qp)), (w, (n, self.n_qp)), (lmin, (n,)), (lmax, (n,))):
+                if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                    raise ValueError("out arrays must be C-contiguous float64 of the right shape")
         vp = None
         if veff is not None:
             veff = np.ascontiguousarray(veff, dtype=np.float64).reshape(-1)
@@ -110,6 +119,21 @@ class LSDFT:
             ctypes.c_void_p(d_lmin), ctypes.c_void_p(d_lmax), ctypes.c_void_p(stream)),
             "sq_nodes_and_weights_device")
 
+    def last_kernel_times(self):
+        """(lanczos_ms, quadrature_ms) of the last nodes-and-weights call (CUDA events)."""
+        ms = np.zeros(2)
+        check(self._lib.sq_last_kernel_times(self._h, _ptr(ms)), "sq_last_kernel_times")
+        return float(ms[0]), float(ms[1])
+
+    def algorithmic_flops_per_node(self):
+        """Useful FP32 FLOPs of one node's Lanczos (n_qp matvecs): per step 2(6o+1) per cube
+        point for the stencil, 1 for Veff, 8 for the recurrence's vector updates and
+        products, and 4 per projector-point-(l,m) for the nonlocal gather and scatter."""
+        nc = self.cube[0] * self.cube[1] * self.cube[2]
+        o = self.info.fd_half_order
+        per_step = (2 * (6 * o + 1) + 1 + 8) * nc + 4 * self.info.n_lm * self.info.proj_points_per_node
+        return self.n_qp * per_step
+
     def sync_status(self, stream=0):
         check(self._lib.sq_sync_status(self._h, ctypes.c_void_p(stream)), "sq_sync_status")
 
@@ -122,14 +146,15 @@ class LSDFT:
         return a, b
 
     # --- Fermi level, density, energy ----------------------------------------------------
-    def CalculateDensity_lssgq(self, lam, weights, n_electrons=None, tol=1e-12):
+    def CalculateDensity_lssgq(self, lam, weights, n_electrons=None, tol=1e-12, rho=None):
         """Fermi level by bisection, node densities, band energy and -TS (FP64)."""
         lam = np.ascontiguousarray(lam, dtype=np.float64)
         weights = np.ascontiguousarray(weights, dtype=np.float64)
         n_nodes = lam.shape[0]
         if n_electrons is None:
             n_electrons = self.n_electrons
-        rho = np.empty(n_nodes)
+        if rho is None:
+            rho = np.empty(n_nodes)
         lf = ctypes.c_double()
         eb = ctypes.c_double()
         ts = ctypes.c_double()

@@ -17,9 +17,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", CSRC,
           "-I", os.path.join(os.path.dirname(HERE), "include")]
 SOURCES = {
-    "lanczos.cu": ["-Xptxas", "-v"],
+    "lanczos.cu": [],
+    "lanczos_f32.cu": ["-Xptxas", "-v"],
+    "lanczos_f64.cu": ["-Xptxas", "-v"],
     "quadrature.cu": ["-fmad=false"],
     "fermi.cu": [],
+    "probe.cu": [],
     "capi.cpp": ["-x", "cu"],
     "setup.cpp": [],
     "deck.cpp": [],

@@ -28,7 +28,8 @@ class SqInfo(ctypes.Structure):
                 ("precision", ctypes.c_int), ("faithful", ctypes.c_int), ("n_nodes", ctypes.c_long),
                 ("h", ctypes.c_double * 3), ("cell_half", ctypes.c_double * 3),
                 ("rcut", ctypes.c_double), ("beta", ctypes.c_double), ("dV", ctypes.c_double),
-                ("n_electrons", ctypes.c_double)]
+                ("n_electrons", ctypes.c_double), ("n_lm", ctypes.c_int),
+                ("proj_points_per_node", ctypes.c_double)]
 
 
 SIGNATURES = {
@@ -45,6 +46,8 @@ SIGNATURES = {
     "sq_fermi_density_energy": (ctypes.c_int, [_vp, _dp, _dp, _l, _d, _d, _dp, _dp, _dp, _dp]),
     "sq_fermi_density_energy_device": (ctypes.c_int, [_vp, _vp, _vp, _l, _d, _d, _dp, _vp, _dp,
                                                       _dp, _vp]),
+    "sq_last_kernel_times": (ctypes.c_int, [_vp, _dp]),
+    "sq_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int, _dp]),
     "sq_last_error_string": (ctypes.c_char_p, []),
 }
 

@@ -55,6 +55,7 @@ struct sq_handle {
   bool u_smem = false;
   size_t smem = 0;
   int grid = 0;
+  int block = 0;
   int fermi_grid = 0;
   size_t elem = 4;
   // device buffers owned by the handle
@@ -76,6 +77,8 @@ struct sq_handle {
   double *d_fermi_out = nullptr;
   int fermi_maxit = 400;
   cudaStream_t own_stream = nullptr;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  bool ev_valid = false;
 
   ~sq_handle() {
     dev_free(d_images);
@@ -93,6 +96,8 @@ struct sq_handle {
     dev_free(d_fermi_scratch);
     dev_free(d_bar);
     dev_free(d_fermi_out);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 };
@@ -149,8 +154,36 @@ void ensure_capacity(double *&ptr, long long &cap, long long need, const char *w
   cap = need;
 }
 
+// Mean over all nodes of sum_images |box ∩ cube|.  The overlap of a box with the cube of
+// node (I,J,K) factorises over the axes, so the sum over the node grid is a product of
+// three 1D sums per image.
+double projector_points_per_node(const sq::Setup &s, const sq::Deck &d) {
+  double total = 0.0;
+  for (const sq::ImageMeta &im : s.images) {
+    const sq::TypeDesc &td = s.types[im.type];
+    const int b[3] = {im.bx, im.by, im.bz}, f[3] = {td.fx, td.fy, td.fz};
+    double prod = 1.0;
+    for (int a = 0; a < 3; a++) {
+      long long sum = 0;
+      for (int I = 0; I < d.grid[a]; I++) {
+        const int lo = std::max(b[a], I - s.nh[a]), hi = std::min(b[a] + f[a] - 1, I + s.nh[a]);
+        if (hi >= lo) sum += hi - lo + 1;
+      }
+      prod *= (double)sum;
+    }
+    total += prod;
+  }
+  return total / ((double)d.grid[0] * d.grid[1] * d.grid[2]);
+}
+
 void fill_info(sq_info &in, const sq::Deck &d, const sq::Setup &s, int max_img,
                const sq_options &opt) {
+  int mask = 0;
+  for (const sq::TypeDesc &t : s.types) mask |= t.chan_mask;
+  in.n_lm = 0;
+  for (int l = 0; l < 4; l++)
+    if (mask & (1 << l)) in.n_lm += 2 * l + 1;
+  in.proj_points_per_node = projector_points_per_node(s, d);
   for (int a = 0; a < 3; a++) {
     in.grid[a] = d.grid[a];
     in.cube[a] = s.cube[a];
@@ -183,6 +216,7 @@ void build_engine(sq_handle *h) {
   ck(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->opt.device),
      "smem optin");
   ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
+  for (auto &e : h->ev) ck(cudaEventCreate(&e), "event");
 
   sq::LanczosParams &p = h->lp;
   p.nx = s.cube[0];
@@ -204,6 +238,9 @@ void build_engine(sq_handle *h) {
   p.hx = s.h[0];
   p.hy = s.h[1];
   p.hz = s.h[2];
+  p.hxf = (float)p.hx;
+  p.hyf = (float)p.hy;
+  p.hzf = (float)p.hz;
   p.cdiag = s.c[0][0] + s.c[1][0] + s.c[2][0];
   p.cdiagf = (float)p.cdiag;
   for (int q = 0; q <= sq::kStencilHalf; q++) {
@@ -219,10 +256,17 @@ void build_engine(sq_handle *h) {
     p.types[t] = s.types[t];
     p.union_mask |= s.types[t].chan_mask;
   }
+  // (l,m) ranks in the order of the instantiated channel mask (sq::lk::Lm<MASK>::rank)
+  const int kmask = sq::kernel_mask(p.union_mask);
   int rank = 0;
   for (int l = 0; l < 4; l++)
-    for (int m = -l; m <= l; m++) p.lm_rank[l * l + l + m] = (p.union_mask & (1 << l)) ? rank++ : -1;
-  p.alpha_stride = h->opt.faithful ? 1 : std::max(rank, 1);
+    for (int m = -l; m <= l; m++) {
+      const int s = l * l + l + m;
+      p.lm_rank[s] = (kmask & (1 << l)) ? rank : -1;
+      if (kmask & (1 << l)) p.rank_l[rank++] = l;
+    }
+  for (int r = rank; r < sq::kMaxLm; r++) p.rank_l[r] = 0;
+  p.alpha_stride = h->opt.faithful ? 1 : rank;
 
   if (p.nx > 32) throw std::invalid_argument("cubes wider than 32 points in x are not supported");
   if (d.n_qp > 64) throw std::invalid_argument("LANCZOS_DEGREE above 64 is not supported");
@@ -230,12 +274,15 @@ void build_engine(sq_handle *h) {
   const int need_img = std::max(1, max_images_per_node(s, d));
   p.max_img = need_img;
   h->elem = h->opt.precision == 32 ? 4 : 8;
-  const int block = h->opt.precision == 32 ? sq::kBlockF32 : sq::kBlockF64;
+  const int maxw = h->opt.precision == 32 ? sq::kMaxWarpsF32 : sq::kMaxWarpsF64;
+  p.rows_per_warp = (p.ny + maxw - 1) / maxw;
+  h->block = 32 * ((p.ny + p.rows_per_warp - 1) / p.rows_per_warp);
+  const bool faithful = h->opt.faithful != 0;
   h->u_smem = false;
   if (h->opt.precision == 32 &&
-      sq::lanczos_smem_bytes(p, 4, true, block) <= (size_t)smem_optin)
+      sq::lanczos_smem_bytes(p, 4, true, faithful) <= (size_t)smem_optin)
     h->u_smem = true;
-  h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, block);
+  h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
   if (h->smem > (size_t)smem_optin)
     throw std::invalid_argument("cube of " + std::to_string(p.nx) + "x" + std::to_string(p.ny) +
                                 "x" + std::to_string(p.nz) +
@@ -296,11 +343,15 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
   ck(cudaMemsetAsync(h->d_status, 0, sizeof(int), s), "status reset");
   ck(sq::launch_veff_extend(d_veff, veff_const, h->d_veff_ext, h->opt.precision, p, s), "veff");
   const int grid = (int)std::min<long long>(h->grid, n);
-  ck(sq::launch_lanczos(p, h->opt.precision, h->opt.faithful != 0, h->u_smem, grid, h->smem, s,
+  ck(cudaEventRecord(h->ev[0], s), "event");
+  ck(sq::launch_lanczos(p, h->opt.precision, h->opt.faithful != 0, h->u_smem, grid, h->block, h->smem, s,
                         h->d_veff_ext, h->d_images, h->d_tables, h->d_u, h->d_ab, h->d_status),
      "lanczos");
+  ck(cudaEventRecord(h->ev[1], s), "event");
   ck(sq::launch_quadrature(h->d_ab, n, p.nqp, d_lambda, d_w, d_lmin, d_lmax, h->d_status, s),
      "quadrature");
+  ck(cudaEventRecord(h->ev[2], s), "event");
+  h->ev_valid = true;
   h->last_n = n;
   return SQ_OK;
 }
@@ -498,6 +549,29 @@ sq_status sq_fermi_density_energy(sq_handle *h, const double *lambda, const doub
       ck(cudaMemcpyAsync(rho, h->d_rho, sizeof(double) * n_nodes, cudaMemcpyDeviceToHost, s), "D2H");
       ck(cudaStreamSynchronize(s), "sync");
     }
+    return SQ_OK;
+  });
+}
+
+sq_status sq_last_kernel_times(sq_handle *h, double *ms) {
+  if (!h || !ms) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    if (!h->ev_valid) return fail(SQ_BAD_INPUT, "no nodes_and_weights call yet");
+    ck(cudaEventSynchronize(h->ev[2]), "event sync");
+    float a = 0, b = 0;
+    ck(cudaEventElapsedTime(&a, h->ev[0], h->ev[1]), "elapsed");
+    ck(cudaEventElapsedTime(&b, h->ev[1], h->ev[2]), "elapsed");
+    ms[0] = a;
+    ms[1] = b;
+    return SQ_OK;
+  });
+}
+
+sq_status sq_measure_fp32_peak(int device, double *tflops) {
+  if (!tflops) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(sq::measure_fp32_peak(device, tflops), "fp32 probe");
     return SQ_OK;
   });
 }

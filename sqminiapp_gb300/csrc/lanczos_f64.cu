@@ -1,0 +1,15 @@
+// lanczos_f64.cu -- FP64-vector instantiations of the Lanczos kernel (U in global scratch).
+#include "lanczos_kernel.cuh"
+
+namespace sq {
+
+cudaError_t launch_lanczos_f64(int mask, bool faithful, const LanczosParams &p, int grid,
+                               int block, size_t smem, cudaStream_t s, const void *veff_ext,
+                               const ImageMeta *images, const void *tables, void *u_scratch,
+                               double *ab, int *status) {
+  if (faithful)
+    return lk::launch_mask<double, true, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+  return lk::launch_mask<double, false, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+}
+
+}  // namespace sq

@@ -1,0 +1,583 @@
+// lanczos_kernel.cuh -- the batched per-node Lanczos kernel (template, sm_103a).
+//
+// Replaces the hot loop of NodesAndWeights_LSSGQ / CalculateSpectralNodesAndWeights
+// (src/lsdft_scf.cc:60-150): for every FD node, n_qp Lanczos steps from the unit vector at
+// the cube centre on H = -1/2 Lap (12th-order FD, Dirichlet cube, src/lsdft_initObjs.cc:393-475)
+// + diag(Veff) + the Kleinman-Bylander projectors of the atom images that meet the cube
+// (src/lsdft_matvec.cc:25-149).
+//
+// Layout.  A persistent CTA owns one node at a time and keeps both Lanczos vectors on chip:
+//   P  the stencil source, rows padded by 6 zeros in x (pitch = nx + 6) so the x-neighbours
+//      of a row need no bounds checks;
+//   U  the elementwise vector (v_{k-1}, then the new residual), unpadded; in shared memory
+//      when both fit, else in a per-CTA slice of global scratch.
+// Vector passes: warp w owns a contiguous block of y-rows and walks z with a 13-value
+// register window (shifted by one each step), so one output costs 12 x-loads + 12 y-loads
+// + 1 z-load of shared memory.
+// Nonlocal term: the points of all (image, box ∩ cube) pairs of the node form one flat index
+// space that is cut into equal per-warp ranges.  The gather accumulates c_lm = <chi_lm, P>
+// per lane, reduces it with shuffles when a range leaves an image and adds it into the
+// image's atom slot with a shared atomic; the scatter adds chi_lm alpha_lm into U with
+// shared atomics.  chi_lm is rebuilt on the fly as T_l(r) P_lm(x,y,z) from the per-atom radial
+// tables (L2 resident) and the real solid harmonics.
+//
+// Recurrence (reference scf.cc:119-147, same quantities, fused passes):
+//   P = b_{k-1} v_k (unnormalised), U = v_{k-1};
+//   pass 1:  h = H P / b_{k-1};  a_k = <v_k, h>;  U <- h - b_{k-1} U
+//   pass 2:  w = U - a_k v_k;    b_k = ||w||;     P <- w;  U <- v_k
+// a_k and b_k are accumulated per thread in the vector precision and summed across the CTA
+// in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <type_traits>
+
+#include "sq_internal.hpp"
+#include "sq_kernels.hpp"
+
+namespace sq {
+namespace lk {
+
+constexpr int O = kStencilHalf;
+constexpr int W = 2 * O + 1;
+constexpr int kMaxWarps = 32;
+
+template <typename T> struct Coef;
+template <> struct Coef<float> {
+  static __device__ __forceinline__ float x(const LanczosParams &p, int d) { return p.cxf[d]; }
+  static __device__ __forceinline__ float y(const LanczosParams &p, int d) { return p.cyf[d]; }
+  static __device__ __forceinline__ float z(const LanczosParams &p, int d) { return p.czf[d]; }
+  static __device__ __forceinline__ float diag(const LanczosParams &p) { return p.cdiagf; }
+};
+template <> struct Coef<double> {
+  static __device__ __forceinline__ double x(const LanczosParams &p, int d) { return p.cx[d]; }
+  static __device__ __forceinline__ double y(const LanczosParams &p, int d) { return p.cy[d]; }
+  static __device__ __forceinline__ double z(const LanczosParams &p, int d) { return p.cz[d]; }
+  static __device__ __forceinline__ double diag(const LanczosParams &p) { return p.cdiag; }
+};
+
+// (l,m) bookkeeping of a channel mask (bit l = nonlocal channel l), slot s = l*l + l + m.
+template <int MASK> struct Lm {
+  static constexpr int nlm = ((MASK & 1) ? 1 : 0) + ((MASK & 2) ? 3 : 0) + ((MASK & 4) ? 5 : 0) +
+                             ((MASK & 8) ? 7 : 0);
+  static __host__ __device__ constexpr int l_of(int s) { return s < 1 ? 0 : (s < 4 ? 1 : (s < 9 ? 2 : 3)); }
+  static __host__ __device__ constexpr int rank(int s) {
+    int base = 0;
+    for (int q = 0; q < l_of(s); q++)
+      if (MASK & (1 << q)) base += 2 * q + 1;
+    return base + (s - l_of(s) * l_of(s));
+  }
+};
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of one double per thread over the CTA (nw warps); red holds kMaxWarps+1 doubles.
+__device__ __forceinline__ double block_sum(double v, double *red, int nw) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  v = warp_sum(v);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double t = lane < nw ? red[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) red[kMaxWarps] = t;
+  }
+  __syncthreads();
+  return red[kMaxWarps];
+}
+
+// Real solid harmonics r^l Y_lm with the reference's constants (src/lsdft_tools.cc:165-187);
+// FN(slot, value) for every m of channel l.  For l = 0 the constant is folded into the table.
+template <int L, typename T, typename FN>
+__device__ __forceinline__ void solid_harmonics(T x, T y, T z, FN &&fn) {
+  if constexpr (L == 0) {
+    fn(0, T(1));
+  } else if constexpr (L == 1) {
+    const T c = T(0.488602511902920);
+    fn(1, c * y);
+    fn(2, c * z);
+    fn(3, c * x);
+  } else if constexpr (L == 2) {
+    fn(4, T(1.092548430592079) * (x * y));
+    fn(5, T(1.092548430592079) * (y * z));
+    fn(6, T(0.315391565252520) * (T(2) * z * z - x * x - y * y));
+    fn(7, T(1.092548430592079) * (z * x));
+    fn(8, T(0.546274215296040) * (x * x - y * y));
+  } else {
+    fn(9, T(0.590043589926644) * (T(3) * x * x - y * y) * y);
+    fn(10, T(2.890611442640554) * (x * y * z));
+    fn(11, T(0.457045799464466) * y * (T(4) * z * z - x * x - y * y));
+    fn(12, T(0.373176332590115) * z * (T(2) * z * z - T(3) * x * x - T(3) * y * y));
+    fn(13, T(0.457045799464466) * x * (T(4) * z * z - x * x - y * y));
+    fn(14, T(1.445305721320277) * z * (x * x - y * y));
+    fn(15, T(0.590043589926644) * x * (x * x - T(3) * y * y));
+  }
+}
+
+template <typename T> __device__ __forceinline__ T hx_of(const LanczosParams &p);
+template <> __device__ __forceinline__ float hx_of<float>(const LanczosParams &p) { return p.hxf; }
+template <> __device__ __forceinline__ double hx_of<double>(const LanczosParams &p) { return p.hx; }
+template <typename T> __device__ __forceinline__ T hy_of(const LanczosParams &p);
+template <> __device__ __forceinline__ float hy_of<float>(const LanczosParams &p) { return p.hyf; }
+template <> __device__ __forceinline__ double hy_of<double>(const LanczosParams &p) { return p.hy; }
+template <typename T> __device__ __forceinline__ T hz_of(const LanczosParams &p);
+template <> __device__ __forceinline__ float hz_of<float>(const LanczosParams &p) { return p.hzf; }
+template <> __device__ __forceinline__ double hz_of<double>(const LanczosParams &p) { return p.hz; }
+
+// Per-image data of the current node, decoded once when a warp range enters an image.
+// Point (lx,ly,lz) of box ∩ cube sits at P[pbase + lz*PS + ly*pitch + lx],
+// U[ubase + (lz*ny + ly)*nx + lx], table entry tab[(lz*fy + ly)*fx + lx], and at
+// coordinates (ox + hx*lx, oy + hy*ly, oz + hz*lz) relative to the image's atom.
+template <typename T> struct ImgView {
+  int pbase, ubase;
+  int ex, ey;
+  float iex, iey;
+  int fx, fxy, fvol;
+  int chan_mask;
+  const T *tab;
+  T ox, oy, oz;
+};
+
+template <typename T>
+__device__ __forceinline__ ImgView<T> load_view(const LanczosParams &p, const ImageMeta *images,
+                                                const T *tables, int gidx, int blo, int bext,
+                                                int Xs, int Ys, int Zs, int OFF, int PS) {
+  ImgView<T> v;
+  const ImageMeta m = images[gidx];
+  const TypeDesc &td = p.types[m.type];
+  const int cx0 = blo & 1023, cy0 = (blo >> 10) & 1023, cz0 = blo >> 20;
+  v.ex = bext & 1023;
+  v.ey = (bext >> 10) & 1023;
+  v.iex = 1.0f / v.ex;
+  v.iey = 1.0f / v.ey;
+  v.pbase = OFF + cz0 * PS + cy0 * p.pitch + cx0;
+  v.ubase = (cz0 * p.ny + cy0) * p.nx + cx0;
+  const int tx0 = Xs + cx0 - m.bx, ty0 = Ys + cy0 - m.by, tz0 = Zs + cz0 - m.bz;
+  v.fx = td.fx;
+  v.fxy = td.fx * td.fy;
+  v.fvol = v.fxy * td.fz;
+  v.chan_mask = td.chan_mask;
+  v.tab = tables + m.tab_base + (tz0 * v.fxy + ty0 * v.fx + tx0);
+  v.ox = T(m.ox + p.hx * tx0);
+  v.oy = T(m.oy + p.hy * ty0);
+  v.oz = T(m.oz + p.hz * tz0);
+  return v;
+}
+
+// Decode point t of the intersection box (x fastest) without integer division.
+template <typename T>
+__device__ __forceinline__ void decode(const ImgView<T> &v, int t, int &lx, int &ly, int &lz) {
+  const int row = __float2int_rz((float(t) + 0.5f) * v.iex);
+  lx = t - row * v.ex;
+  lz = __float2int_rz((float(row) + 0.5f) * v.iey);
+  ly = row - lz * v.ey;
+}
+
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD>
+__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
+    lanczos_kernel(const __grid_constant__ LanczosParams p, const T *__restrict__ veff_ext,
+                   const ImageMeta *__restrict__ images, const T *__restrict__ tables,
+                   T *__restrict__ u_global, double *__restrict__ ab_out, int *__restrict__ status) {
+  constexpr int NLM = Lm<MASK>::nlm;
+  constexpr int CSTRIDE = FAITHFUL ? 2 : NLM;  // gather accumulators per atom slot
+  constexpr int ASTRIDE = FAITHFUL ? 1 : NLM;  // projector coefficients per atom slot
+  const int nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
+  // P index of (x,y,z) = OFF + z*PS + y*pitch + x.  YPAD: every z-plane carries O zero rows
+  // above and below, so y-neighbours need no bounds checks either.
+  const int PS = (YPAD ? ny + 2 * O : ny) * pitch;
+  const int OFF = YPAD ? O * pitch : O;
+  const int US = ny * nx;  // U plane stride
+  const int nc = nz * ny * nx;
+  const int psize = ((OFF + nz * PS) + 3) & ~3;
+  const int maxi = p.max_img;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *P = reinterpret_cast<T *>(smem_raw);
+  T *U;
+  unsigned char *cur = smem_raw + sizeof(T) * psize;
+  if constexpr (U_SMEM) {
+    U = reinterpret_cast<T *>(cur);
+    cur += sizeof(T) * ((nc + 3) & ~3);
+  } else {
+    U = u_global + (size_t)blockIdx.x * (size_t)((nc + 3) & ~3);
+  }
+  double *red = reinterpret_cast<double *>(cur);  // 2 x (kMaxWarps+1)
+  cur += sizeof(double) * 2 * (kMaxWarps + 1);
+  double *sab = reinterpret_cast<double *>(cur);  // a[64], b[64]
+  cur += sizeof(double) * 128;
+  T *cacc = reinterpret_cast<T *>(cur);
+  cur += sizeof(T) * maxi * CSTRIDE;
+  T *alpha = reinterpret_cast<T *>(cur);
+  cur += sizeof(T) * maxi * ASTRIDE;
+  int *img = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * maxi;
+  int *slot = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * maxi;
+  int *slot_type = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * maxi;
+  int *blo = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * maxi;
+  int *bext = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * maxi;
+  int *pref = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * (maxi + 1);
+  int *cnt = reinterpret_cast<int *>(cur);  // [0] images, [1] slots, [2] overflow
+
+  const int x = lane;
+  const bool xin = x < nx;
+  const int xc = xin ? x : nx - 1;
+  const int y_begin = warp * p.rows_per_warp;
+  const int y_end = min(ny, y_begin + p.rows_per_warp);
+
+  for (long long node = p.node_begin + blockIdx.x; node < p.node_end; node += gridDim.x) {
+    const int I = (int)(node % p.Nx);
+    const int J = (int)((node / p.Nx) % p.Ny);
+    const int K = (int)(node / ((long long)p.Nx * p.Ny));
+    const int Xs = I - p.nhx, Ys = J - p.nhy, Zs = K - p.nhz;
+
+    // ---- per-node image list, slots and point offsets (warp 0); others clear ----
+    if (warp == 0) {
+      int count = 0;
+      for (int base = 0; base < p.n_images; base += 32) {
+        const int i = base + lane;
+        bool ok = false;
+        if (i < p.n_images) {
+          const int4 b = *reinterpret_cast<const int4 *>(&images[i]);
+          const TypeDesc &td = p.types[b.w];
+          ok = b.x <= Xs + nx - 1 && b.x + td.fx - 1 >= Xs && b.y <= Ys + ny - 1 &&
+               b.y + td.fy - 1 >= Ys && b.z <= Zs + nz - 1 && b.z + td.fz - 1 >= Zs;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        const int pos = count + __popc(m & ((1u << lane) - 1u));
+        if (ok && pos < maxi) img[pos] = i;
+        count += __popc(m);
+      }
+      __syncwarp();
+      const int n = min(count, maxi);
+      int slots = 0, offset = 0;
+      for (int base = 0; base < n; base += 32) {
+        const int k = base + lane;
+        bool start = false;
+        int npts = 0, lo = 0, ext = 0, atom = -1, type = 0;
+        if (k < n) {
+          const ImageMeta m = images[img[k]];
+          atom = m.atom;
+          type = m.type;
+          start = (k == 0) || images[img[k - 1]].atom != atom;
+          const TypeDesc &td = p.types[m.type];
+          const int x0 = max(m.bx, Xs), y0 = max(m.by, Ys), z0 = max(m.bz, Zs);
+          const int ex = min(m.bx + td.fx, Xs + nx) - x0;
+          const int ey = min(m.by + td.fy, Ys + ny) - y0;
+          const int ez = min(m.bz + td.fz, Zs + nz) - z0;
+          npts = ex * ey * ez;
+          lo = (x0 - Xs) | ((y0 - Ys) << 10) | ((z0 - Zs) << 20);
+          ext = ex | (ey << 10) | (ez << 20);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, start);
+        const int g = slots + __popc(m & ((1u << lane) - 1u)) + (start ? 0 : -1);
+        int incl = npts;  // inclusive scan of npts
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (k < n) {
+          slot[k] = g;
+          if (start) slot_type[g] = type;
+          blo[k] = lo;
+          bext[k] = ext;
+          pref[k] = offset + incl - npts;
+        }
+        slots += __popc(m);
+        offset += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) {
+        pref[n] = offset;
+        cnt[0] = n;
+        cnt[1] = slots;
+        cnt[2] = count > maxi;
+      }
+    } else {
+      for (int e = threadIdx.x - 32; e < psize; e += blockDim.x - 32) P[e] = T(0);
+      for (int e = threadIdx.x - 32; e < nc; e += blockDim.x - 32) U[e] = T(0);
+      for (int e = threadIdx.x - 32; e < maxi * CSTRIDE; e += blockDim.x - 32) cacc[e] = T(0);
+    }
+    __syncthreads();
+    const int n_img = cnt[0], n_slot = cnt[1];
+    if (cnt[2]) {  // capacity exceeded: report and leave NaN coefficients for this node
+      if (threadIdx.x == 0) atomicOr(status, kStatusCapacity);
+      for (int j = threadIdx.x; j < 2 * p.nqp; j += blockDim.x)
+        ab_out[(node - p.node_begin) * 2 * p.nqp + j] = __longlong_as_double(0x7ff8000000000000ll);
+      __syncthreads();
+      continue;
+    }
+    if (threadIdx.x == 0) P[OFF + (nz - 1) / 2 * PS + (ny - 1) / 2 * pitch + (nx - 1) / 2] = T(1);
+    const int total = pref[n_img];
+    const int per = (total + nw - 1) / nw;
+    const int r_begin = min(total, warp * per), r_end = min(total, r_begin + per);
+    int k_first = 0;  // image containing r_begin: largest k with pref[k] <= r_begin
+    {
+      int lo = 0, hi = n_img;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pref[mid] <= r_begin) lo = mid;
+        else hi = mid - 1;
+      }
+      k_first = min(lo, max(n_img - 1, 0));
+    }
+    __syncthreads();
+
+    double beta = 1.0;
+    for (int j = 0; j < p.nqp; j++) {
+      const T inv = T(1.0 / beta);
+      const T tbeta = T(beta);
+
+      // ---- nonlocal gather over this warp's range of projector points ----
+      {
+        int pos = r_begin, k = k_first;
+        while (pos < r_end) {
+          const int kend = min(r_end, pref[k + 1]);
+          const ImgView<T> v = load_view<T>(p, images, tables, img[k], blo[k], bext[k], Xs, Ys, Zs, OFF, PS);
+          T acc[CSTRIDE];
+#pragma unroll
+          for (int s = 0; s < CSTRIDE; s++) acc[s] = T(0);
+          T gam[4];
+          if constexpr (FAITHFUL) {
+            const TypeDesc &td = p.types[slot_type[slot[k]]];
+#pragma unroll
+            for (int l = 0; l < 4; l++) gam[l] = T(td.gamma[l]);
+          }
+          for (int q = pos + lane - pref[k]; q < kend - pref[k]; q += 32) {
+            int lx, ly, lz;
+            decode(v, q, lx, ly, lz);
+            const T val = P[v.pbase + lz * PS + ly * pitch + lx];
+            const T dx = v.ox + hx_of<T>(p) * T(lx), dy = v.oy + hy_of<T>(p) * T(ly),
+                    dz = v.oz + hz_of<T>(p) * T(lz);
+            const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
+            int chan = 0;
+            auto channel = [&](auto Lc) {
+              constexpr int L = decltype(Lc)::value;
+              if constexpr (MASK & (1 << L)) {
+                if (v.chan_mask & (1 << L)) {
+                  const T tv = tb[(chan++) * v.fvol] * val;
+                  if constexpr (FAITHFUL) {
+                    T ssum = T(0);
+                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) { ssum += ylm; });
+                    acc[0] += gam[L] * ssum * tv;
+                    acc[1] += ssum * tv;
+                  } else {
+                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) {
+                      acc[Lm<MASK>::rank(s)] += ylm * tv;
+                    });
+                  }
+                }
+              }
+            };
+            channel(std::integral_constant<int, 0>{});
+            channel(std::integral_constant<int, 1>{});
+            channel(std::integral_constant<int, 2>{});
+            channel(std::integral_constant<int, 3>{});
+          }
+          const int sl = slot[k];
+#pragma unroll
+          for (int s = 0; s < CSTRIDE; s++) {
+            const T r = warp_sum(acc[s]);
+            if (lane == 0) atomicAdd(&cacc[sl * CSTRIDE + s], r);
+          }
+          pos = kend;
+          k++;
+        }
+      }
+      __syncthreads();
+
+      // ---- projector coefficients alpha from the gathered c, plus <v, V_nl v> ----
+      double a_part = 0.0;
+      for (int e = threadIdx.x; e < n_slot * ASTRIDE; e += blockDim.x) {
+        if constexpr (FAITHFUL) {
+          const double cg = (double)cacc[2 * e] * (double)inv;
+          const double cs = (double)cacc[2 * e + 1] * (double)inv;
+          cacc[2 * e] = T(0);
+          cacc[2 * e + 1] = T(0);
+          alpha[e] = T(cg);
+          a_part += cs * cg;
+        } else {
+          const int sl = e / NLM, r = e - sl * NLM;
+          const TypeDesc &td = p.types[slot_type[sl]];
+          const int l = p.rank_l[r];
+          const double c = (double)cacc[e] * (double)inv;
+          cacc[e] = T(0);
+          const double gl = (td.chan_mask & (1 << l)) ? td.gamma[l] : 0.0;
+          alpha[e] = T(gl * c);
+          a_part += gl * c * c;
+        }
+      }
+
+      // ---- pass 1: stencil + Veff, U <- H v_k - b_{k-1} U, a_k partial ----
+      T a_acc = T(0);
+      for (int y = y_begin; y < y_end; y++) {
+        const int rowP = OFF + y * pitch + xc;
+        const int rowU = y * nx + xc;
+        const T *vrow = veff_ext + ((size_t)K * p.EY + (J + y)) * p.EX + (I + xc);
+        const size_t VS = (size_t)p.EY * p.EX;
+        T win[W];
+#pragma unroll
+        for (int q = -O; q < O; q++)
+          win[q + O + 1] = (q >= 0 && q < nz) ? P[rowP + min(max(q, 0), nz - 1) * PS] : T(0);
+#pragma unroll 1
+        for (int z = 0; z < nz; z++) {
+#pragma unroll
+          for (int t = 0; t < W - 1; t++) win[t] = win[t + 1];
+          const int qn = z + O;
+          win[W - 1] = (qn < nz) ? P[rowP + min(qn, nz - 1) * PS] : T(0);
+          const int i = rowP + z * PS;
+          const T vc = win[O];
+          T h = (Coef<T>::diag(p) + vrow[z * VS]) * vc;
+#pragma unroll
+          for (int d = 1; d <= O; d++) {
+            h += Coef<T>::z(p, d) * (win[O - d] + win[O + d]);
+            h += Coef<T>::x(p, d) * (P[i - d] + P[i + d]);
+            if constexpr (YPAD) {
+              h += Coef<T>::y(p, d) * (P[i - d * pitch] + P[i + d * pitch]);
+            } else {  // rows outside the cube are zero: clamp the index, then drop the value
+              const T ym = P[y - d >= 0 ? i - d * pitch : i];
+              const T yp = P[y + d < ny ? i + d * pitch : i];
+              h += Coef<T>::y(p, d) * ((y - d >= 0 ? ym : T(0)) + (y + d < ny ? yp : T(0)));
+            }
+          }
+          h *= inv;
+          if (xin) {
+            const int u = rowU + z * US;
+            a_acc += (vc * inv) * h;
+            U[u] = h - tbeta * U[u];
+          }
+        }
+      }
+      __syncthreads();
+
+      // ---- nonlocal scatter over this warp's range: U += sum_lm chi_lm alpha_lm ----
+      {
+        int pos = r_begin, k = k_first;
+        while (pos < r_end) {
+          const int kend = min(r_end, pref[k + 1]);
+          const ImgView<T> v = load_view<T>(p, images, tables, img[k], blo[k], bext[k], Xs, Ys, Zs, OFF, PS);
+          const T *al = alpha + slot[k] * ASTRIDE;
+          T coef[ASTRIDE];
+#pragma unroll
+          for (int s = 0; s < ASTRIDE; s++) coef[s] = al[s];
+          for (int q = pos + lane - pref[k]; q < kend - pref[k]; q += 32) {
+            int lx, ly, lz;
+            decode(v, q, lx, ly, lz);
+            const T dx = v.ox + hx_of<T>(p) * T(lx), dy = v.oy + hy_of<T>(p) * T(ly),
+                    dz = v.oz + hz_of<T>(p) * T(lz);
+            const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
+            T val = T(0);
+            int chan = 0;
+            auto channel = [&](auto Lc) {
+              constexpr int L = decltype(Lc)::value;
+              if constexpr (MASK & (1 << L)) {
+                if (v.chan_mask & (1 << L)) {
+                  const T tv = tb[(chan++) * v.fvol];
+                  T sum = T(0);
+                  if constexpr (FAITHFUL) {
+                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) { sum += ylm; });
+                    val += tv * sum * coef[0];
+                  } else {
+                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) {
+                      sum += ylm * coef[Lm<MASK>::rank(s)];
+                    });
+                    val += tv * sum;
+                  }
+                }
+              }
+            };
+            channel(std::integral_constant<int, 0>{});
+            channel(std::integral_constant<int, 1>{});
+            channel(std::integral_constant<int, 2>{});
+            channel(std::integral_constant<int, 3>{});
+            atomicAdd(&U[v.ubase + (lz * ny + ly) * nx + lx], val);
+          }
+          pos = kend;
+          k++;
+        }
+      }
+      const double a = block_sum((double)a_acc + a_part, red, nw);
+
+      // ---- pass 2: w = U - a_k v_k, P <- w, U <- v_k, b_k = ||w|| ----
+      const T ta = T(a);
+      T b_acc = T(0);
+      if (xin) {
+        for (int y = y_begin; y < y_end; y++) {
+          const int rowP = OFF + y * pitch + x;
+          const int rowU = y * nx + x;
+          for (int z = 0; z < nz; z++) {
+            const T pv = P[rowP + z * PS];
+            const T vk = pv * inv;
+            const T w = U[rowU + z * US] - ta * vk;
+            P[rowP + z * PS] = w;
+            U[rowU + z * US] = vk;
+            b_acc += w * w;
+          }
+        }
+      }
+      const double b = sqrt(block_sum((double)b_acc, red + kMaxWarps + 1, nw));
+      if (threadIdx.x == 0) {
+        sab[j] = a;
+        sab[64 + j] = b;
+      }
+      if (!(b > 0.0) || !isfinite(b)) {  // breakdown: the Krylov space is invariant
+        if (threadIdx.x == 0) {
+          atomicOr(status, kStatusBreakdown);
+          for (int r = j + 1; r < p.nqp; r++) {
+            sab[r] = 0.0;
+            sab[64 + r] = 0.0;
+          }
+        }
+        break;
+      }
+      beta = b;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < p.nqp; r += blockDim.x) {
+      double *o = ab_out + (node - p.node_begin) * 2 * p.nqp;
+      o[r] = sab[r];
+      o[p.nqp + r] = sab[64 + r];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK>
+cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t smem,
+                           cudaStream_t s, const void *veff_ext, const ImageMeta *images,
+                           const void *tables, void *u_scratch, double *ab, int *status) {
+  constexpr bool YPAD = sizeof(T) == 4;  // FP32 pads y; FP64 does not fit padded
+  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, block, smem, s>>>(p, (const T *)veff_ext, images, (const T *)tables, (T *)u_scratch,
+                              ab, status);
+  return cudaGetLastError();
+}
+
+template <typename T, bool FAITHFUL, bool U_SMEM>
+cudaError_t launch_mask(int mask, const LanczosParams &p, int grid, int block, size_t smem,
+                        cudaStream_t s, const void *veff_ext, const ImageMeta *images,
+                        const void *tables, void *u_scratch, double *ab, int *status) {
+  switch (mask) {
+    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+    default: return launch_variant<T, FAITHFUL, U_SMEM, 15>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+  }
+}
+
+}  // namespace lk
+}  // namespace sq

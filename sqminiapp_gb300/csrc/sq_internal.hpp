@@ -53,9 +53,12 @@ struct LanczosParams {
   int alpha_stride;        // coefficients per image slot (number of (l,m) of the mask union)
   int union_mask;          // bit l set if any type has a nonlocal channel l
   int lm_rank[kMaxLm];     // compact slot of (l,m) in alpha_stride, -1 if absent
+  int rank_l[kMaxLm];      // l of compact slot r
   int ntype;
+  int rows_per_warp;       // cube y-rows owned by one warp in the vector passes
   long long node_begin, node_end;
   double hx, hy, hz;
+  float hxf, hyf, hzf;
   double cdiag;            // coeffs_x[0] + coeffs_y[0] + coeffs_z[0]
   double cx[kStencilHalf + 1], cy[kStencilHalf + 1], cz[kStencilHalf + 1];
   float cdiagf;            // FP32 copies for the FP32 engine

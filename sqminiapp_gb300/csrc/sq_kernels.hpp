@@ -9,8 +9,8 @@
 
 namespace sq {
 
-constexpr int kBlockF32 = 1024;  // one CTA per SM, 32 warps
-constexpr int kBlockF64 = 512;   // FP64 register window needs more registers per thread
+constexpr int kMaxWarpsF32 = 32;  // one CTA per SM, up to 32 warps (64 registers/thread)
+constexpr int kMaxWarpsF64 = 16;  // FP64 register window needs up to 128 registers/thread
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;
@@ -18,10 +18,14 @@ constexpr int kStatusBreakdown = 2;
 constexpr int kStatusNoConvergence = 4;
 constexpr int kStatusTimeout = 8;
 
-size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, int block);
+// channel mask the kernel is instantiated for (union mask, or 15 = generic) and its (l,m) count
+int kernel_mask(int union_mask);
+int mask_nlm(int mask);
+
+size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bool faithful);
 
 cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful, bool u_smem,
-                           int grid, size_t smem, cudaStream_t s, const void *veff_ext,
+                           int grid, int block, size_t smem, cudaStream_t s, const void *veff_ext,
                            const ImageMeta *images, const void *tables, void *u_scratch,
                            double *ab, int *status);
 
@@ -39,5 +43,8 @@ cudaError_t launch_fermi(const double *lambda, const double *w, long long n_node
                          double beta, double n_electrons, double dV, double tol, int maxit,
                          double *rho, double *out, double *scratch, unsigned *barrier,
                          int *status, int grid, cudaStream_t s);
+
+// FP32 FMA throughput of `device` in TFLOP/s (register-resident FMA chains on every SM).
+cudaError_t measure_fp32_peak(int device, double *tflops);
 
 }  // namespace sq
