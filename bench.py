@@ -51,6 +51,8 @@ def parse_args():
                    help="CPU time budget of the cpu_baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--max-nodes", type=int, default=0,
+                   help="process only the first N nodes per step (profiling of small cases)")
     return p.parse_args()
 
 
@@ -187,9 +189,11 @@ def run_ours(args):
     (deck_dir, name, meta), cfg = make_deck(args.config, rank)
     eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local)
     n, q = eng.n_nodes, eng.n_qp
+    if args.max_nodes > 0:
+        n = min(n, args.max_nodes)
     dev = torch.device("cuda", local)
     rng = np.random.default_rng(11 + rank)
-    veff_host = (-0.2 + 0.05 * rng.standard_normal(n)).astype(np.float64)
+    veff_host = (-0.2 + 0.05 * rng.standard_normal(eng.n_nodes)).astype(np.float64)
     veff = torch.from_numpy(veff_host).to(dev)
     lam = torch.empty((n, q), dtype=torch.float64, device=dev)
     wts = torch.empty((n, q), dtype=torch.float64, device=dev)
@@ -260,17 +264,17 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         pin = lambda shape: torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-        hv = pin(n)
+        hv = pin(eng.n_nodes)
         hv[:] = veff_host
         out = {"lambda": pin((n, q)), "weights": pin((n, q)), "lambda_min": pin(n),
                "lambda_max": pin(n)}
         hrho = pin(n)
-        eng.NodesAndWeights_LSSGQ(veff=hv, out=out)
+        eng.NodesAndWeights_LSSGQ(veff=hv, node_end=n, out=out)
         if world > 1:
             dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            eng.NodesAndWeights_LSSGQ(veff=hv, out=out)
+            eng.NodesAndWeights_LSSGQ(veff=hv, node_end=n, out=out)
             eng.CalculateDensity_lssgq(out["lambda"], out["weights"], rho=hrho)
         e2e_s = time.perf_counter() - t0
         te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)

@@ -11,7 +11,7 @@
 #include <stdexcept>
 #include <string>
 
-#include "../../include/sq_gb300.h"
+#include "sq_gb300.h"
 #include "sq_internal.hpp"
 #include "sq_kernels.hpp"
 
@@ -64,6 +64,7 @@ struct sq_handle {
   void *d_veff_ext = nullptr;
   double *d_veff_in = nullptr;
   void *d_u = nullptr;
+  void *d_proj = nullptr;
   int *d_status = nullptr;
   double *d_ab = nullptr;
   long long ab_cap = 0;
@@ -86,6 +87,7 @@ struct sq_handle {
     dev_free(d_veff_ext);
     dev_free(d_veff_in);
     dev_free(d_u);
+    dev_free(d_proj);
     dev_free(d_status);
     dev_free(d_ab);
     dev_free(d_lambda);
@@ -144,6 +146,38 @@ int max_images_per_node(const sq::Setup &s, const sq::Deck &d) {
         at(x, y, z) = v;
         if (x < N[0] && y < N[1] && z < N[2]) best = std::max(best, v);
       }
+  return best;
+}
+
+// Largest number of (image, box point) pairs inside one node's cube.  The overlap of an image
+// box with the cube of node (I,J,K) is a product of three 1D overlaps, so every image adds
+// ov_x(I) ov_y(J) ov_z(K) over the nodes whose cubes it meets.
+long long max_box_points_per_node(const sq::Setup &s, const sq::Deck &d) {
+  const int N[3] = {d.grid[0], d.grid[1], d.grid[2]};
+  std::vector<long long> acc((size_t)N[0] * N[1] * N[2], 0);
+  for (const sq::ImageMeta &im : s.images) {
+    const sq::TypeDesc &td = s.types[im.type];
+    const int b[3] = {im.bx, im.by, im.bz}, f[3] = {td.fx, td.fy, td.fz};
+    std::vector<int> ov[3];
+    int lo[3];
+    bool empty = false;
+    for (int a = 0; a < 3; a++) {
+      lo[a] = std::max(0, b[a] - s.nh[a]);
+      const int hi = std::min(N[a] - 1, b[a] + f[a] - 1 + s.nh[a]);
+      if (hi < lo[a]) empty = true;
+      for (int I = lo[a]; I <= hi; I++)
+        ov[a].push_back(std::min(b[a] + f[a] - 1, I + s.nh[a]) - std::max(b[a], I - s.nh[a]) + 1);
+    }
+    if (empty) continue;
+    for (size_t kz = 0; kz < ov[2].size(); kz++)
+      for (size_t jy = 0; jy < ov[1].size(); jy++) {
+        const long long yz = (long long)ov[1][jy] * ov[2][kz];
+        long long *row = &acc[((size_t)(lo[2] + kz) * N[1] + (lo[1] + jy)) * N[0] + lo[0]];
+        for (size_t ix = 0; ix < ov[0].size(); ix++) row[ix] += yz * ov[0][ix];
+      }
+  }
+  long long best = 0;
+  for (long long v : acc) best = std::max(best, v);
   return best;
 }
 
@@ -288,6 +322,17 @@ void build_engine(sq_handle *h) {
                                 "x" + std::to_string(p.nz) +
                                 " does not fit in shared memory at this precision");
   h->grid = h->num_sms;
+  {  // projector records pack the P and U indices of a cube point into 16 bits each
+    const long long pitch_rows = (h->opt.precision == 32) ? p.ny + 2 * sq::kStencilHalf : p.ny;
+    const long long psize = (long long)sq::kStencilHalf * p.pitch + (long long)p.nz * pitch_rows * p.pitch;
+    if (psize >= 65536 || (long long)p.nx * p.ny * p.nz >= 65536)
+      throw std::invalid_argument("truncated cube too large for 16-bit point indices");
+  }
+  const long long cap = std::max(1LL, max_box_points_per_node(s, d));
+  if (cap > (1LL << 31) - 1) throw std::invalid_argument("projector list too large");
+  p.proj_cap = (int)cap;
+  p.proj_bytes_per_cta =
+      (long long)((cap * sq::proj_record_bytes((int)h->elem, faithful, p.union_mask) + 255) & ~255LL);
 
   // device buffers
   dev_alloc(&h->d_images, sizeof(sq::ImageMeta) * s.images.size(), "images");
@@ -307,6 +352,7 @@ void build_engine(sq_handle *h) {
     const size_t nc4 = ((size_t)p.nx * p.ny * p.nz + 3) & ~size_t(3);
     dev_alloc(&h->d_u, h->elem * nc4 * h->grid, "U scratch");
   }
+  dev_alloc(&h->d_proj, (size_t)p.proj_bytes_per_cta * h->grid, "projector list scratch");
   dev_alloc(&h->d_status, sizeof(int) * 4, "status");
   ck(cudaMemset(h->d_status, 0, sizeof(int) * 4), "status memset");
   h->fermi_grid = h->num_sms;
@@ -345,7 +391,8 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
   const int grid = (int)std::min<long long>(h->grid, n);
   ck(cudaEventRecord(h->ev[0], s), "event");
   ck(sq::launch_lanczos(p, h->opt.precision, h->opt.faithful != 0, h->u_smem, grid, h->block, h->smem, s,
-                        h->d_veff_ext, h->d_images, h->d_tables, h->d_u, h->d_ab, h->d_status),
+                        h->d_veff_ext, h->d_images, h->d_tables, h->d_u, h->d_proj, h->d_ab,
+                        h->d_status),
      "lanczos");
   ck(cudaEventRecord(h->ev[1], s), "event");
   ck(sq::launch_quadrature(h->d_ab, n, p.nqp, d_lambda, d_w, d_lmin, d_lmax, h->d_status, s),

@@ -32,6 +32,12 @@ int kernel_mask(int union_mask) {
   return (union_mask == 3 || union_mask == 5 || union_mask == 6 || union_mask == 7) ? union_mask : 15;
 }
 
+size_t proj_record_bytes(int elem_size, bool faithful, int union_mask) {
+  const int n = faithful ? 2 : mask_nlm(kernel_mask(union_mask));
+  const int per_vec = 16 / elem_size;
+  return (size_t)16 * ((n + per_vec - 1) / per_vec) + sizeof(unsigned);
+}
+
 int mask_nlm(int mask) {
   int n = 0;
   for (int l = 0; l < 4; l++)
@@ -51,29 +57,29 @@ size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bo
   if (u_smem) b += elem_size * ((nc + 3) & ~size_t(3));
   b += sizeof(double) * 2 * (lk::kMaxWarps + 1) + sizeof(double) * 128;
   b += (size_t)elem_size * p.max_img * (cstride + astride);
-  b += sizeof(int) * (6 * (size_t)p.max_img + 1) + sizeof(int) * 4;
+  b += sizeof(int) * (8 * (size_t)p.max_img + 2) + sizeof(int) * 4;
   return b;
 }
 
 cudaError_t launch_lanczos_f32(int mask, bool faithful, bool u_smem, const LanczosParams &p,
                                int grid, int block, size_t smem, cudaStream_t s,
                                const void *veff_ext, const ImageMeta *images, const void *tables,
-                               void *u_scratch, double *ab, int *status);
+                               void *u_scratch, void *proj_scratch, double *ab, int *status);
 cudaError_t launch_lanczos_f64(int mask, bool faithful, const LanczosParams &p, int grid,
                                int block, size_t smem, cudaStream_t s, const void *veff_ext,
                                const ImageMeta *images, const void *tables, void *u_scratch,
-                               double *ab, int *status);
+                               void *proj_scratch, double *ab, int *status);
 
 cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful, bool u_smem,
                            int grid, int block, size_t smem, cudaStream_t s, const void *veff_ext,
                            const ImageMeta *images, const void *tables, void *u_scratch,
-                           double *ab, int *status) {
+                           void *proj_scratch, double *ab, int *status) {
   const int mask = kernel_mask(p.union_mask);
   if (precision == 32)
     return launch_lanczos_f32(mask, faithful, u_smem, p, grid, block, smem, s, veff_ext, images,
-                              tables, u_scratch, ab, status);
+                              tables, u_scratch, proj_scratch, ab, status);
   return launch_lanczos_f64(mask, faithful, p, grid, block, smem, s, veff_ext, images, tables,
-                            u_scratch, ab, status);
+                            u_scratch, proj_scratch, ab, status);
 }
 
 cudaError_t launch_veff_extend(const double *veff, double vconst, void *ext, int precision,

@@ -6,10 +6,10 @@ namespace sq {
 cudaError_t launch_lanczos_f64(int mask, bool faithful, const LanczosParams &p, int grid,
                                int block, size_t smem, cudaStream_t s, const void *veff_ext,
                                const ImageMeta *images, const void *tables, void *u_scratch,
-                               double *ab, int *status) {
+                               void *proj_scratch, double *ab, int *status) {
   if (faithful)
-    return lk::launch_mask<double, true, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
-  return lk::launch_mask<double, false, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+    return lk::launch_mask<double, true, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+  return lk::launch_mask<double, false, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
 }
 
 }  // namespace sq

@@ -129,6 +129,54 @@ template <typename T> __device__ __forceinline__ T hz_of(const LanczosParams &p)
 template <> __device__ __forceinline__ float hz_of<float>(const LanczosParams &p) { return p.hzf; }
 template <> __device__ __forceinline__ double hz_of<double>(const LanczosParams &p) { return p.hz; }
 
+template <typename T> __device__ __forceinline__ T support_r2(const TypeDesc &td);
+template <> __device__ __forceinline__ float support_r2<float>(const TypeDesc &td) { return td.support_r2_f32; }
+template <> __device__ __forceinline__ double support_r2<double>(const TypeDesc &td) { return td.support_r2_f64; }
+
+// One record of the per-node projector list: N values of T (chi_lm, or for the reference's
+// shared-slot operator sum_lm Gamma_l chi_lm and sum_lm chi_lm), padded to whole 16-byte
+// vectors so a warp streams the list with 128-bit loads.
+template <typename T, int N> struct ProjRec {
+  static constexpr int n = N;
+  static constexpr int per_vec = 16 / (int)sizeof(T);
+  static constexpr int nvec = (N + per_vec - 1) / per_vec;
+  using vec_t = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  static __device__ __forceinline__ void store(vec_t *rec, int e, const T *v) {
+    T tmp[nvec * per_vec];
+#pragma unroll
+    for (int s = 0; s < nvec * per_vec; s++) tmp[s] = s < N ? v[s] : T(0);
+#pragma unroll
+    for (int j = 0; j < nvec; j++) {
+      vec_t x;
+      if constexpr (sizeof(T) == 4) {
+        x.x = tmp[4 * j]; x.y = tmp[4 * j + 1]; x.z = tmp[4 * j + 2]; x.w = tmp[4 * j + 3];
+      } else {
+        x.x = tmp[2 * j]; x.y = tmp[2 * j + 1];
+      }
+      rec[(size_t)e * nvec + j] = x;
+    }
+  }
+  static __device__ __forceinline__ void load(const vec_t *rec, int e, T *c) {
+#pragma unroll
+    for (int j = 0; j < nvec; j++) {
+      const vec_t x = rec[(size_t)e * nvec + j];
+      T t[per_vec];
+      if constexpr (sizeof(T) == 4) {
+        t[0] = x.x; t[1] = x.y; t[2] = x.z; t[3] = x.w;
+      } else {
+        t[0] = x.x; t[1] = x.y;
+      }
+#pragma unroll
+      for (int s = 0; s < per_vec; s++)
+        if (j * per_vec + s < N) c[j * per_vec + s] = t[s];
+    }
+  }
+};
+
+template <typename T, bool FAITHFUL, int MASK> constexpr int rec_values() {
+  return FAITHFUL ? 2 : Lm<MASK>::nlm;
+}
+
 // Per-image data of the current node, decoded once when a warp range enters an image.
 // Point (lx,ly,lz) of box ∩ cube sits at P[pbase + lz*PS + ly*pitch + lx],
 // U[ubase + (lz*ny + ly)*nx + lx], table entry tab[(lz*fy + ly)*fx + lx], and at
@@ -141,6 +189,7 @@ template <typename T> struct ImgView {
   int chan_mask;
   const T *tab;
   T ox, oy, oz;
+  T r2max;  // projector support radius squared
 };
 
 template <typename T>
@@ -166,6 +215,7 @@ __device__ __forceinline__ ImgView<T> load_view(const LanczosParams &p, const Im
   v.ox = T(m.ox + p.hx * tx0);
   v.oy = T(m.oy + p.hy * ty0);
   v.oz = T(m.oz + p.hz * tz0);
+  v.r2max = support_r2<T>(td);
   return v;
 }
 
@@ -182,8 +232,10 @@ template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD>
 __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
     lanczos_kernel(const __grid_constant__ LanczosParams p, const T *__restrict__ veff_ext,
                    const ImageMeta *__restrict__ images, const T *__restrict__ tables,
-                   T *__restrict__ u_global, double *__restrict__ ab_out, int *__restrict__ status) {
+                   T *__restrict__ u_global, unsigned char *proj_scratch,
+                   double *__restrict__ ab_out, int *__restrict__ status) {
   constexpr int NLM = Lm<MASK>::nlm;
+  using Rec = ProjRec<T, FAITHFUL ? 2 : NLM>;
   constexpr int CSTRIDE = FAITHFUL ? 2 : NLM;  // gather accumulators per atom slot
   constexpr int ASTRIDE = FAITHFUL ? 1 : NLM;  // projector coefficients per atom slot
   const int nw = blockDim.x >> 5;
@@ -228,7 +280,17 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
   cur += sizeof(int) * maxi;
   int *pref = reinterpret_cast<int *>(cur);
   cur += sizeof(int) * (maxi + 1);
+  int *kept = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * maxi;
+  int *koff = reinterpret_cast<int *>(cur);
+  cur += sizeof(int) * (maxi + 1);
   int *cnt = reinterpret_cast<int *>(cur);  // [0] images, [1] slots, [2] overflow
+
+  // this CTA's slice of the per-node projector list (records, then packed P|U indices)
+  typename Rec::vec_t *rec = reinterpret_cast<typename Rec::vec_t *>(
+      proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
+  unsigned *ridx = reinterpret_cast<unsigned *>(
+      reinterpret_cast<unsigned char *>(rec) + (size_t)p.proj_cap * sizeof(typename Rec::vec_t) * Rec::nvec);
 
   const int x = lane;
   const bool xin = x < nx;
@@ -319,15 +381,100 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
       continue;
     }
     if (threadIdx.x == 0) P[OFF + (nz - 1) / 2 * PS + (ny - 1) / 2 * pitch + (nx - 1) / 2] = T(1);
-    const int total = pref[n_img];
+    if (pref[n_img] > p.proj_cap) {  // cannot happen with the host's capacity; guard anyway
+      if (threadIdx.x == 0) atomicOr(status, kStatusCapacity);
+      for (int j = threadIdx.x; j < 2 * p.nqp; j += blockDim.x)
+        ab_out[(node - p.node_begin) * 2 * p.nqp + j] = __longlong_as_double(0x7ff8000000000000ll);
+      __syncthreads();
+      continue;
+    }
+
+    // ---- build this node's projector list: one warp per image, support points only ----
+    // Record e of image k sits at e = pref[k] + (rank among the image's kept points) and holds
+    // chi_lm (or, faithful, sum_lm Gamma_l chi_lm and sum_lm chi_lm) and the packed P|U index.
+    for (int kk = warp; kk < n_img; kk += nw) {
+      const ImgView<T> v = load_view<T>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, OFF, PS);
+      T gam[4];
+      {
+        const TypeDesc &td = p.types[slot_type[slot[kk]]];
+#pragma unroll
+        for (int l = 0; l < 4; l++) gam[l] = T(td.gamma[l]);
+      }
+      const int npts = pref[kk + 1] - pref[kk];
+      int kept_n = 0;
+      for (int q0 = 0; q0 < npts; q0 += 32) {
+        const int q = q0 + lane;
+        int lx, ly, lz;
+        decode(v, min(q, npts - 1), lx, ly, lz);
+        const T dx = v.ox + hx_of<T>(p) * T(lx), dy = v.oy + hy_of<T>(p) * T(ly),
+                dz = v.oz + hz_of<T>(p) * T(lz);
+        const bool ok = q < npts && dx * dx + dy * dy + dz * dz <= v.r2max;
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+          const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
+          T out[Rec::n];
+#pragma unroll
+          for (int s = 0; s < Rec::n; s++) out[s] = T(0);
+          int chan = 0;
+          auto channel = [&](auto Lc) {
+            constexpr int L = decltype(Lc)::value;
+            if constexpr (MASK & (1 << L)) {
+              if (v.chan_mask & (1 << L)) {
+                const T t = tb[(chan++) * v.fvol];
+                if constexpr (FAITHFUL) {
+                  T ssum = T(0);
+                  solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) { ssum += ylm; });
+                  out[0] += gam[L] * ssum * t;
+                  out[1] += ssum * t;
+                } else {
+                  solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) {
+                    out[Lm<MASK>::rank(s)] = ylm * t;
+                  });
+                }
+              }
+            }
+          };
+          channel(std::integral_constant<int, 0>{});
+          channel(std::integral_constant<int, 1>{});
+          channel(std::integral_constant<int, 2>{});
+          channel(std::integral_constant<int, 3>{});
+          const int e = pref[kk] + kept_n + __popc(m & ((1u << lane) - 1u));
+          Rec::store(rec, e, out);
+          const int pi = v.pbase + lz * PS + ly * pitch + lx;
+          const int ui = v.ubase + (lz * ny + ly) * nx + lx;
+          ridx[e] = (unsigned)pi | ((unsigned)ui << 16);
+        }
+        kept_n += __popc(m);
+      }
+      if (lane == 0) kept[kk] = kept_n;
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of kept -> koff
+      int offset = 0;
+      for (int base = 0; base < n_img; base += 32) {
+        const int kk = base + lane;
+        const int c = kk < n_img ? kept[kk] : 0;
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (kk < n_img) koff[kk] = offset + incl - c;
+        offset += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) koff[n_img] = offset;
+    }
+    __syncthreads();
+    const int total = koff[n_img];
     const int per = (total + nw - 1) / nw;
     const int r_begin = min(total, warp * per), r_end = min(total, r_begin + per);
-    int k_first = 0;  // image containing r_begin: largest k with pref[k] <= r_begin
+    int k_first = 0;  // image holding kept point r_begin: largest k with koff[k] <= r_begin
     {
       int lo = 0, hi = n_img;
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (pref[mid] <= r_begin) lo = mid;
+        if (koff[mid] <= r_begin) lo = mid;
         else hi = mid - 1;
       }
       k_first = min(lo, max(n_img - 1, 0));
@@ -339,55 +486,27 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
       const T inv = T(1.0 / beta);
       const T tbeta = T(beta);
 
-      // ---- nonlocal gather over this warp's range of projector points ----
+      // ---- nonlocal gather: stream this warp's range of the projector list ----
       {
         int pos = r_begin, k = k_first;
         while (pos < r_end) {
-          const int kend = min(r_end, pref[k + 1]);
-          const ImgView<T> v = load_view<T>(p, images, tables, img[k], blo[k], bext[k], Xs, Ys, Zs, OFF, PS);
-          T acc[CSTRIDE];
+          const int kend = min(r_end, koff[k + 1]);
+          const int shift = pref[k] - koff[k];  // list position of kept point i is i + shift
+          T acc[Rec::n];
 #pragma unroll
-          for (int s = 0; s < CSTRIDE; s++) acc[s] = T(0);
-          T gam[4];
-          if constexpr (FAITHFUL) {
-            const TypeDesc &td = p.types[slot_type[slot[k]]];
+          for (int s = 0; s < Rec::n; s++) acc[s] = T(0);
+#pragma unroll 4
+          for (int i = pos + lane; i < kend; i += 32) {
+            const int e = i + shift;
+            T c[Rec::n];
+            Rec::load(rec, e, c);
+            const T val = P[ridx[e] & 0xffffu];
 #pragma unroll
-            for (int l = 0; l < 4; l++) gam[l] = T(td.gamma[l]);
-          }
-          for (int q = pos + lane - pref[k]; q < kend - pref[k]; q += 32) {
-            int lx, ly, lz;
-            decode(v, q, lx, ly, lz);
-            const T val = P[v.pbase + lz * PS + ly * pitch + lx];
-            const T dx = v.ox + hx_of<T>(p) * T(lx), dy = v.oy + hy_of<T>(p) * T(ly),
-                    dz = v.oz + hz_of<T>(p) * T(lz);
-            const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
-            int chan = 0;
-            auto channel = [&](auto Lc) {
-              constexpr int L = decltype(Lc)::value;
-              if constexpr (MASK & (1 << L)) {
-                if (v.chan_mask & (1 << L)) {
-                  const T tv = tb[(chan++) * v.fvol] * val;
-                  if constexpr (FAITHFUL) {
-                    T ssum = T(0);
-                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) { ssum += ylm; });
-                    acc[0] += gam[L] * ssum * tv;
-                    acc[1] += ssum * tv;
-                  } else {
-                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) {
-                      acc[Lm<MASK>::rank(s)] += ylm * tv;
-                    });
-                  }
-                }
-              }
-            };
-            channel(std::integral_constant<int, 0>{});
-            channel(std::integral_constant<int, 1>{});
-            channel(std::integral_constant<int, 2>{});
-            channel(std::integral_constant<int, 3>{});
+            for (int s = 0; s < Rec::n; s++) acc[s] += c[s] * val;
           }
           const int sl = slot[k];
 #pragma unroll
-          for (int s = 0; s < CSTRIDE; s++) {
+          for (int s = 0; s < Rec::n; s++) {
             const T r = warp_sum(acc[s]);
             if (lane == 0) atomicAdd(&cacc[sl * CSTRIDE + s], r);
           }
@@ -461,47 +580,30 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
       }
       __syncthreads();
 
-      // ---- nonlocal scatter over this warp's range: U += sum_lm chi_lm alpha_lm ----
+      // ---- nonlocal scatter: U += sum_lm chi_lm alpha_lm over this warp's range ----
       {
         int pos = r_begin, k = k_first;
         while (pos < r_end) {
-          const int kend = min(r_end, pref[k + 1]);
-          const ImgView<T> v = load_view<T>(p, images, tables, img[k], blo[k], bext[k], Xs, Ys, Zs, OFF, PS);
+          const int kend = min(r_end, koff[k + 1]);
+          const int shift = pref[k] - koff[k];
           const T *al = alpha + slot[k] * ASTRIDE;
           T coef[ASTRIDE];
 #pragma unroll
           for (int s = 0; s < ASTRIDE; s++) coef[s] = al[s];
-          for (int q = pos + lane - pref[k]; q < kend - pref[k]; q += 32) {
-            int lx, ly, lz;
-            decode(v, q, lx, ly, lz);
-            const T dx = v.ox + hx_of<T>(p) * T(lx), dy = v.oy + hy_of<T>(p) * T(ly),
-                    dz = v.oz + hz_of<T>(p) * T(lz);
-            const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
-            T val = T(0);
-            int chan = 0;
-            auto channel = [&](auto Lc) {
-              constexpr int L = decltype(Lc)::value;
-              if constexpr (MASK & (1 << L)) {
-                if (v.chan_mask & (1 << L)) {
-                  const T tv = tb[(chan++) * v.fvol];
-                  T sum = T(0);
-                  if constexpr (FAITHFUL) {
-                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) { sum += ylm; });
-                    val += tv * sum * coef[0];
-                  } else {
-                    solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) {
-                      sum += ylm * coef[Lm<MASK>::rank(s)];
-                    });
-                    val += tv * sum;
-                  }
-                }
-              }
-            };
-            channel(std::integral_constant<int, 0>{});
-            channel(std::integral_constant<int, 1>{});
-            channel(std::integral_constant<int, 2>{});
-            channel(std::integral_constant<int, 3>{});
-            atomicAdd(&U[v.ubase + (lz * ny + ly) * nx + lx], val);
+#pragma unroll 4
+          for (int i = pos + lane; i < kend; i += 32) {
+            const int e = i + shift;
+            T c[Rec::n];
+            Rec::load(rec, e, c);
+            T val;
+            if constexpr (FAITHFUL) {
+              val = c[1] * coef[0];
+            } else {
+              val = T(0);
+#pragma unroll
+              for (int s = 0; s < Rec::n; s++) val += c[s] * coef[s];
+            }
+            atomicAdd(&U[ridx[e] >> 16], val);
           }
           pos = kend;
           k++;
@@ -556,26 +658,28 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
 template <typename T, bool FAITHFUL, bool U_SMEM, int MASK>
 cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t smem,
                            cudaStream_t s, const void *veff_ext, const ImageMeta *images,
-                           const void *tables, void *u_scratch, double *ab, int *status) {
+                           const void *tables, void *u_scratch, void *proj_scratch, double *ab,
+                           int *status) {
   constexpr bool YPAD = sizeof(T) == 4;  // FP32 pads y; FP64 does not fit padded
   auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<grid, block, smem, s>>>(p, (const T *)veff_ext, images, (const T *)tables, (T *)u_scratch,
-                              ab, status);
+                              (unsigned char *)proj_scratch, ab, status);
   return cudaGetLastError();
 }
 
 template <typename T, bool FAITHFUL, bool U_SMEM>
 cudaError_t launch_mask(int mask, const LanczosParams &p, int grid, int block, size_t smem,
                         cudaStream_t s, const void *veff_ext, const ImageMeta *images,
-                        const void *tables, void *u_scratch, double *ab, int *status) {
+                        const void *tables, void *u_scratch, void *proj_scratch, double *ab,
+                        int *status) {
   switch (mask) {
-    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
-    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
-    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
-    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
-    default: return launch_variant<T, FAITHFUL, U_SMEM, 15>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, ab, status);
+    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    default: return launch_variant<T, FAITHFUL, U_SMEM, 15>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
   }
 }
 

@@ -143,6 +143,9 @@ Setup build_setup(const Deck &d, bool faithful) {
       td.chan_off[l] = -1;
       td.gamma[l] = 0.0;
     }
+    td.support_r2_f64 = 0.0;
+    td.support_r2_f32 = 0.0f;
+    td.pad_ = 0;
     rcnl[t] = std::max(std::max(p.rc[0], p.rc[1]), std::max(p.rc[2], p.rc[3]));
     int off[3];
     for (int a = 0; a < 3; a++) off[a] = (int)ceil(rcnl[t] / s.h[a]);
@@ -174,6 +177,29 @@ Setup build_setup(const Deck &d, bool faithful) {
       td.gamma[l] = 1.0 / D;
       td.chan_mask |= 1 << l;
       td.chan_off[l] = nch++;
+    }
+
+    // Support radius of the projectors.  U_l (V_l - V_loc) vanishes beyond rc on the psd grid,
+    // but the cubic spline rings for a few knots past the last nonzero one; scan down from the
+    // box corner for the radius where every channel first exceeds the threshold.
+    {
+      double corner = 0.0;
+      for (int a = 0; a < 3; a++) corner += (off[a] + 1) * s.h[a] * (off[a] + 1) * s.h[a];
+      corner = sqrt(corner);
+      double smax[4] = {0, 0, 0, 0};
+      for (int l = 0; l < 4; l++)
+        if (td.chan_mask & (1 << l))
+          for (double r = 0.0; r <= corner; r += 1e-3) smax[l] = std::max(smax[l], fabs(proj[t][l][0](r)));
+      auto radius_for = [&](double thr) {
+        for (double r = corner; r > 0.0; r -= 1e-3)
+          for (int l = 0; l < 4; l++)
+            if ((td.chan_mask & (1 << l)) && fabs(proj[t][l][0](r)) > thr * smax[l])
+              return std::min(corner, r + 0.05);
+        return 0.05;
+      };
+      const double r64 = radius_for(1e-16), r32 = radius_for(1e-12);
+      td.support_r2_f64 = r64 * r64;
+      td.support_r2_f32 = (float)(r32 * r32);
     }
 
     // pseudocharge cutoff: b = -(1/4pi) Lap V_loc on an octant grid, radius grown by 1 bohr

@@ -38,6 +38,11 @@ struct TypeDesc {
   int chan_mask;           // bit l set if channel l is nonlocal
   int chan_off[4];         // table channel index of l (only if in mask)
   double gamma[4];         // Gamma_l (src/lsdft_initObjs.cc:822-869)
+  // Squared projector support radius (bohr^2): beyond it every |S_l(r)| is below 1e-16 (FP64
+  // engine) or 1e-12 (FP32 engine) of its maximum, i.e. below the arithmetic's own rounding.
+  double support_r2_f64;
+  float support_r2_f32;
+  int pad_;
 };
 
 // Everything the Lanczos kernel reads besides the buffers.
@@ -56,6 +61,8 @@ struct LanczosParams {
   int rank_l[kMaxLm];      // l of compact slot r
   int ntype;
   int rows_per_warp;       // cube y-rows owned by one warp in the vector passes
+  int proj_cap;            // records of one CTA's projector list (max box points of a node)
+  long long proj_bytes_per_cta;
   long long node_begin, node_end;
   double hx, hy, hz;
   float hxf, hyf, hzf;

@@ -24,10 +24,13 @@ int mask_nlm(int mask);
 
 size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bool faithful);
 
+// bytes of one record of the per-node projector list (values + packed P|U index)
+size_t proj_record_bytes(int elem_size, bool faithful, int union_mask);
+
 cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful, bool u_smem,
                            int grid, int block, size_t smem, cudaStream_t s, const void *veff_ext,
                            const ImageMeta *images, const void *tables, void *u_scratch,
-                           double *ab, int *status);
+                           void *proj_scratch, double *ab, int *status);
 
 cudaError_t launch_veff_extend(const double *veff, double vconst, void *ext, int precision,
                                const LanczosParams &p, cudaStream_t s);
