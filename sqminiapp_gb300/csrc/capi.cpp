@@ -265,7 +265,13 @@ void build_engine(sq_handle *h) {
   p.EX = p.Nx + 2 * p.nhx;
   p.EY = p.Ny + 2 * p.nhy;
   p.EZ = p.Nz + 2 * p.nhz;
+  // FP32 vector passes work on aligned x pairs: even row pitches for P and U
   p.pitch = p.nx + sq::kStencilHalf;
+  p.upitch = p.nx;
+  if (h->opt.precision == 32) {
+    p.pitch += p.pitch & 1;
+    p.upitch += p.upitch & 1;
+  }
   p.nqp = d.n_qp;
   p.n_images = (int)s.images.size();
   p.ntype = (int)s.types.size();
@@ -325,7 +331,7 @@ void build_engine(sq_handle *h) {
   {  // projector records pack the P and U indices of a cube point into 16 bits each
     const long long pitch_rows = (h->opt.precision == 32) ? p.ny + 2 * sq::kStencilHalf : p.ny;
     const long long psize = (long long)sq::kStencilHalf * p.pitch + (long long)p.nz * pitch_rows * p.pitch;
-    if (psize >= 65536 || (long long)p.nx * p.ny * p.nz >= 65536)
+    if (psize >= 65536 || (long long)p.upitch * p.ny * p.nz >= 65536)
       throw std::invalid_argument("truncated cube too large for 16-bit point indices");
   }
   const long long cap = std::max(1LL, max_box_points_per_node(s, d));
@@ -349,7 +355,7 @@ void build_engine(sq_handle *h) {
   dev_alloc(&h->d_veff_ext, h->elem * (size_t)p.EX * p.EY * p.EZ, "veff_ext");
   dev_alloc(&h->d_veff_in, sizeof(double) * (size_t)p.Nx * p.Ny * p.Nz, "veff");
   if (!h->u_smem) {
-    const size_t nc4 = ((size_t)p.nx * p.ny * p.nz + 3) & ~size_t(3);
+    const size_t nc4 = ((size_t)p.upitch * p.ny * p.nz + 3) & ~size_t(3);
     dev_alloc(&h->d_u, h->elem * nc4 * h->grid, "U scratch");
   }
   dev_alloc(&h->d_proj, (size_t)p.proj_bytes_per_cta * h->grid, "projector list scratch");

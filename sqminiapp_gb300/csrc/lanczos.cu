@@ -50,7 +50,7 @@ size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bo
   const size_t ps = (size_t)(ypad ? p.ny + 2 * lk::O : p.ny) * p.pitch;
   const size_t off = ypad ? (size_t)lk::O * p.pitch : lk::O;
   const size_t psize = (off + p.nz * ps + 3) & ~size_t(3);
-  const size_t nc = (size_t)p.nx * p.ny * p.nz;
+  const size_t nc = (size_t)p.upitch * p.ny * p.nz;
   const int nlm = mask_nlm(kernel_mask(p.union_mask));
   const size_t cstride = faithful ? 2 : nlm, astride = faithful ? 1 : nlm;
   size_t b = elem_size * psize;

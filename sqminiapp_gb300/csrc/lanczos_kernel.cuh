@@ -6,20 +6,23 @@
 // + diag(Veff) + the Kleinman-Bylander projectors of the atom images that meet the cube
 // (src/lsdft_matvec.cc:25-149).
 //
-// Layout.  A persistent CTA owns one node at a time and keeps both Lanczos vectors on chip:
-//   P  the stencil source, rows padded by 6 zeros in x (pitch = nx + 6) so the x-neighbours
-//      of a row need no bounds checks;
-//   U  the elementwise vector (v_{k-1}, then the new residual), unpadded; in shared memory
-//      when both fit, else in a per-CTA slice of global scratch.
-// Vector passes: warp w owns a contiguous block of y-rows and walks z with a 13-value
-// register window (shifted by one each step), so one output costs 12 x-loads + 12 y-loads
-// + 1 z-load of shared memory.
-// Nonlocal term: the points of all (image, box ∩ cube) pairs of the node form one flat index
-// space that is cut into equal per-warp ranges.  The gather accumulates c_lm = <chi_lm, P>
-// per lane, reduces it with shuffles when a range leaves an image and adds it into the
-// image's atom slot with a shared atomic; the scatter adds chi_lm alpha_lm into U with
-// shared atomics.  chi_lm is rebuilt on the fly as T_l(r) P_lm(x,y,z) from the per-atom radial
-// tables (L2 resident) and the real solid harmonics.
+// Layout.  A persistent CTA (one per SM) owns one node at a time and keeps both Lanczos
+// vectors on chip:
+//   P  the stencil source, with 6 zero columns between rows (x) and, in FP32, 6 zero rows
+//      above and below every z-plane (y), so no neighbour load needs a bounds check;
+//   U  the elementwise vector (v_{k-1}, then the new residual); in shared memory when both
+//      fit, else in a per-CTA slice of global scratch.
+// Vector passes (FP32): a half-warp owns one y-row and a z-range; each lane computes the x
+// pair (x, x+1) from 64-bit shared loads, forming neighbour sums with Blackwell's packed
+// add.rn.f32x2, and walks z with a 13-plane register ring, so one output costs ~10 shared
+// loads.  FP64 uses one warp per row with scalar loads.
+// Nonlocal term: when a node starts, its projector matrix restricted to the cube (support
+// points only) is written once to a per-CTA list in global scratch: per point the packed
+// P/U indices and chi_lm (chi_lm = T_l(r) P_lm(x,y,z), from the per-atom radial tables and
+// the real solid harmonics).  Every Lanczos step then streams that list twice, cut into
+// equal per-warp ranges: the gather accumulates c_lm = <chi_lm, P> per lane and adds the
+// shuffle-reduced sums into the atom's slot with shared atomics when a range leaves an
+// image; the scatter adds sum_lm chi_lm alpha_lm into U with shared atomics.
 //
 // Recurrence (reference scf.cc:119-147, same quantities, fused passes):
 //   P = b_{k-1} v_k (unnormalised), U = v_{k-1};
@@ -119,6 +122,19 @@ __device__ __forceinline__ void solid_harmonics(T x, T y, T z, FN &&fn) {
   }
 }
 
+// Blackwell packed FP32: two adds in one instruction (PTX add.rn.f32x2, sm_100+).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  unsigned long long ra = *reinterpret_cast<unsigned long long *>(&a);
+  unsigned long long rb = *reinterpret_cast<unsigned long long *>(&b);
+  unsigned long long rd;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  return *reinterpret_cast<float2 *>(&rd);
+}
+__device__ __forceinline__ void fma2s(float2 &h, float c, float2 s) {
+  h.x = fmaf(c, s.x, h.x);
+  h.y = fmaf(c, s.y, h.y);
+}
+
 template <typename T> __device__ __forceinline__ T hx_of(const LanczosParams &p);
 template <> __device__ __forceinline__ float hx_of<float>(const LanczosParams &p) { return p.hxf; }
 template <> __device__ __forceinline__ double hx_of<double>(const LanczosParams &p) { return p.hx; }
@@ -173,6 +189,10 @@ template <typename T, int N> struct ProjRec {
   }
 };
 
+// Points per lane per batch of the projector-list streaming loops: 8 for records of up to
+// 16 bytes, fewer for wider records so the batch stays in registers.
+template <int BYTES> __host__ __device__ constexpr int stream_batch() { return BYTES <= 16 ? 8 : (BYTES <= 32 ? 4 : 2); }
+
 template <typename T, bool FAITHFUL, int MASK> constexpr int rec_values() {
   return FAITHFUL ? 2 : Lm<MASK>::nlm;
 }
@@ -205,7 +225,7 @@ __device__ __forceinline__ ImgView<T> load_view(const LanczosParams &p, const Im
   v.iex = 1.0f / v.ex;
   v.iey = 1.0f / v.ey;
   v.pbase = OFF + cz0 * PS + cy0 * p.pitch + cx0;
-  v.ubase = (cz0 * p.ny + cy0) * p.nx + cx0;
+  v.ubase = (cz0 * p.ny + cy0) * p.upitch + cx0;
   const int tx0 = Xs + cx0 - m.bx, ty0 = Ys + cy0 - m.by, tz0 = Zs + cz0 - m.bz;
   v.fx = td.fx;
   v.fxy = td.fx * td.fy;
@@ -229,13 +249,14 @@ __device__ __forceinline__ void decode(const ImgView<T> &v, int t, int &lx, int 
 }
 
 template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD>
-__global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
+__global__ void __launch_bounds__(512, 1)
     lanczos_kernel(const __grid_constant__ LanczosParams p, const T *__restrict__ veff_ext,
                    const ImageMeta *__restrict__ images, const T *__restrict__ tables,
                    T *__restrict__ u_global, unsigned char *proj_scratch,
                    double *__restrict__ ab_out, int *__restrict__ status) {
   constexpr int NLM = Lm<MASK>::nlm;
   using Rec = ProjRec<T, FAITHFUL ? 2 : NLM>;
+  constexpr int kStream = stream_batch<Rec::n * (int)sizeof(T)>();
   constexpr int CSTRIDE = FAITHFUL ? 2 : NLM;  // gather accumulators per atom slot
   constexpr int ASTRIDE = FAITHFUL ? 1 : NLM;  // projector coefficients per atom slot
   const int nw = blockDim.x >> 5;
@@ -245,8 +266,9 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
   // above and below, so y-neighbours need no bounds checks either.
   const int PS = (YPAD ? ny + 2 * O : ny) * pitch;
   const int OFF = YPAD ? O * pitch : O;
-  const int US = ny * nx;  // U plane stride
-  const int nc = nz * ny * nx;
+  const int upitch = p.upitch;  // U row pitch (nx, or nx+1 to keep FP32 pairs aligned)
+  const int US = ny * upitch;   // U plane stride
+  const int nc = nz * US;       // U elements including the row padding
   const int psize = ((OFF + nz * PS) + 3) & ~3;
   const int maxi = p.max_img;
 
@@ -297,6 +319,18 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
   const int xc = xin ? x : nx - 1;
   const int y_begin = warp * p.rows_per_warp;
   const int y_end = min(ny, y_begin + p.rows_per_warp);
+  // FP32 vector passes: half-warp hw owns row py and a z-chunk [zb, ze); lane hl owns the x
+  // pair (px, px+1) with px even.  pact = the pair has a cube point, phi = so does px+1.
+  constexpr bool PAIRED = YPAD;
+  const int hw = threadIdx.x >> 4, hl = threadIdx.x & 15;
+  const int nzs = max(1, (2 * nw) / ny);
+  const int py = hw / nzs, zc = hw - (hw / nzs) * nzs;
+  const int zlen = (nz + nzs - 1) / nzs;
+  const int zb = zc * zlen, ze = min(nz, zb + zlen);
+  const int px = 2 * hl;
+  const bool pact = PAIRED && py < ny && px < nx && zb < ze;
+  const int phi = (px + 1 < nx) ? 1 : 0;
+  const int pxc = px < nx ? px : ((nx - 1) & ~1);
 
   for (long long node = p.node_begin + blockIdx.x; node < p.node_end; node += gridDim.x) {
     const int I = (int)(node % p.Nx);
@@ -441,7 +475,7 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
           const int e = pref[kk] + kept_n + __popc(m & ((1u << lane) - 1u));
           Rec::store(rec, e, out);
           const int pi = v.pbase + lz * PS + ly * pitch + lx;
-          const int ui = v.ubase + (lz * ny + ly) * nx + lx;
+          const int ui = v.ubase + (lz * ny + ly) * upitch + lx;
           ridx[e] = (unsigned)pi | ((unsigned)ui << 16);
         }
         kept_n += __popc(m);
@@ -495,14 +529,24 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
           T acc[Rec::n];
 #pragma unroll
           for (int s = 0; s < Rec::n; s++) acc[s] = T(0);
-#pragma unroll 4
-          for (int i = pos + lane; i < kend; i += 32) {
-            const int e = i + shift;
-            T c[Rec::n];
-            Rec::load(rec, e, c);
-            const T val = P[ridx[e] & 0xffffu];
+          // batches of kStream points per lane: all list loads of a batch are issued before
+          // any is used (addresses clamped into the segment), so each warp keeps
+          // 2*kStream L2 requests in flight
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
+            T c[kStream][Rec::n];
+            unsigned ix[kStream];
 #pragma unroll
-            for (int s = 0; s < Rec::n; s++) acc[s] += c[s] * val;
+            for (int u = 0; u < kStream; u++) {
+              const int e = min(i0 + 32 * u, kend - 1) + shift;
+              ix[u] = ridx[e];
+              Rec::load(rec, e, c[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kStream; u++) {
+              const T val = (i0 + 32 * u < kend) ? P[ix[u] & 0xffffu] : T(0);
+#pragma unroll
+              for (int s = 0; s < Rec::n; s++) acc[s] += c[u][s] * val;
+            }
           }
           const int sl = slot[k];
 #pragma unroll
@@ -540,41 +584,111 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
 
       // ---- pass 1: stencil + Veff, U <- H v_k - b_{k-1} U, a_k partial ----
       T a_acc = T(0);
-      for (int y = y_begin; y < y_end; y++) {
-        const int rowP = OFF + y * pitch + xc;
-        const int rowU = y * nx + xc;
-        const T *vrow = veff_ext + ((size_t)K * p.EY + (J + y)) * p.EX + (I + xc);
-        const size_t VS = (size_t)p.EY * p.EX;
-        T win[W];
+      if constexpr (PAIRED) {
+        // half-warp item (row py, z-chunk); lane pair x = px, px+1 (px even)
+        const float2 *P2 = reinterpret_cast<const float2 *>(P);
+        float2 *U2 = reinterpret_cast<float2 *>(U);
+        const int PS2 = PS >> 1, pitch2 = pitch >> 1, US2 = US >> 1;
+        const int VS = p.EY * p.EX;
+        if (pact) {
+          const int rowP2 = (OFF + py * pitch + pxc) >> 1;
+          const int rowU2 = (py * upitch + pxc) >> 1;
+          const float *vrow = veff_ext + ((size_t)K * p.EY + (J + py)) * p.EX + (I + pxc);
+          const float2 zero2 = make_float2(0.f, 0.f);
+          float2 win[W];
 #pragma unroll
-        for (int q = -O; q < O; q++)
-          win[q + O + 1] = (q >= 0 && q < nz) ? P[rowP + min(max(q, 0), nz - 1) * PS] : T(0);
-#pragma unroll 1
-        for (int z = 0; z < nz; z++) {
+          for (int q = -O; q < O; q++) {
+            const int zq = zb + q;
+            win[q + O + 1] = (zq >= 0 && zq < nz) ? P2[rowP2 + min(max(zq, 0), nz - 1) * PS2] : zero2;
+          }
+          // ring window: plane z + d lives in win[(z - zb + d + O + 1) % W]; the 13-step
+          // unroll keeps every index static so the window never moves between registers
+          for (int z0 = zb; z0 < ze; z0 += W) {
 #pragma unroll
-          for (int t = 0; t < W - 1; t++) win[t] = win[t + 1];
-          const int qn = z + O;
-          win[W - 1] = (qn < nz) ? P[rowP + min(qn, nz - 1) * PS] : T(0);
-          const int i = rowP + z * PS;
-          const T vc = win[O];
-          T h = (Coef<T>::diag(p) + vrow[z * VS]) * vc;
-#pragma unroll
-          for (int d = 1; d <= O; d++) {
-            h += Coef<T>::z(p, d) * (win[O - d] + win[O + d]);
-            h += Coef<T>::x(p, d) * (P[i - d] + P[i + d]);
-            if constexpr (YPAD) {
-              h += Coef<T>::y(p, d) * (P[i - d * pitch] + P[i + d * pitch]);
-            } else {  // rows outside the cube are zero: clamp the index, then drop the value
-              const T ym = P[y - d >= 0 ? i - d * pitch : i];
-              const T yp = P[y + d < ny ? i + d * pitch : i];
-              h += Coef<T>::y(p, d) * ((y - d >= 0 ? ym : T(0)) + (y + d < ny ? yp : T(0)));
+            for (int s = 0; s < W; s++) {
+              const int z = z0 + s;
+              if (z >= ze) break;
+              const int qn = z + O;
+              win[s] = (qn < nz) ? P2[rowP2 + min(qn, nz - 1) * PS2] : zero2;
+#define WIN(dd) win[(s + (dd) + O + 1) % W]
+              const int i2 = rowP2 + z * PS2;
+              float2 L[7];  // x-6 .. x+7
+  #pragma unroll
+              for (int jx = 0; jx < 7; jx++) L[jx] = P2[i2 - 3 + jx];
+              const float2 vc = WIN(0);
+              float2 hz, hx, hy;
+              hz.x = (p.cdiagf + vrow[z * VS]) * vc.x;
+              hz.y = (p.cdiagf + vrow[z * VS + phi]) * vc.y;
+              hx = zero2;
+              hy = zero2;
+  #pragma unroll
+              for (int d = 1; d <= O; d++) {
+                fma2s(hz, p.czf[d], add2(WIN(-d), WIN(d)));
+                fma2s(hy, p.cyf[d], add2(P2[i2 - d * pitch2], P2[i2 + d * pitch2]));
+                if (d % 2 == 0) {
+                  fma2s(hx, p.cxf[d], add2(L[3 - d / 2], L[3 + d / 2]));
+                } else {
+                  const float2 s = make_float2(L[(5 - d) / 2].y + L[(5 + d) / 2].y,
+                                               L[(7 - d) / 2].x + L[(7 + d) / 2].x);
+                  fma2s(hx, p.cxf[d], s);
+                }
+              }
+              float2 h = add2(add2(hz, hx), hy);
+              h.x *= inv;
+              h.y *= inv;
+              const int u2 = rowU2 + z * US2;
+              const float2 uo = U2[u2];
+              a_acc += (vc.x * inv) * h.x;
+              float2 un;
+              un.x = h.x - tbeta * uo.x;
+              un.y = 0.f;
+              if (phi) {
+                a_acc += (vc.y * inv) * h.y;
+                un.y = h.y - tbeta * uo.y;
+              }
+              U2[u2] = un;
+
+#undef WIN
             }
           }
-          h *= inv;
-          if (xin) {
-            const int u = rowU + z * US;
-            a_acc += (vc * inv) * h;
-            U[u] = h - tbeta * U[u];
+        }
+      } else {
+        for (int y = y_begin; y < y_end; y++) {
+          const int rowP = OFF + y * pitch + xc;
+          const int rowU = y * upitch + xc;
+          const T *vrow = veff_ext + ((size_t)K * p.EY + (J + y)) * p.EX + (I + xc);
+          const size_t VS = (size_t)p.EY * p.EX;
+          T win[W];
+  #pragma unroll
+          for (int q = -O; q < O; q++)
+            win[q + O + 1] = (q >= 0 && q < nz) ? P[rowP + min(max(q, 0), nz - 1) * PS] : T(0);
+  #pragma unroll 1
+          for (int z = 0; z < nz; z++) {
+  #pragma unroll
+            for (int t = 0; t < W - 1; t++) win[t] = win[t + 1];
+            const int qn = z + O;
+            win[W - 1] = (qn < nz) ? P[rowP + min(qn, nz - 1) * PS] : T(0);
+            const int i = rowP + z * PS;
+            const T vc = win[O];
+            T h = (Coef<T>::diag(p) + vrow[z * VS]) * vc;
+  #pragma unroll
+            for (int d = 1; d <= O; d++) {
+              h += Coef<T>::z(p, d) * (win[O - d] + win[O + d]);
+              h += Coef<T>::x(p, d) * (P[i - d] + P[i + d]);
+              if constexpr (YPAD) {
+                h += Coef<T>::y(p, d) * (P[i - d * pitch] + P[i + d * pitch]);
+              } else {  // rows outside the cube are zero: clamp the index, then drop the value
+                const T ym = P[y - d >= 0 ? i - d * pitch : i];
+                const T yp = P[y + d < ny ? i + d * pitch : i];
+                h += Coef<T>::y(p, d) * ((y - d >= 0 ? ym : T(0)) + (y + d < ny ? yp : T(0)));
+              }
+            }
+            h *= inv;
+            if (xin) {
+              const int u = rowU + z * US;
+              a_acc += (vc * inv) * h;
+              U[u] = h - tbeta * U[u];
+            }
           }
         }
       }
@@ -590,20 +704,27 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
           T coef[ASTRIDE];
 #pragma unroll
           for (int s = 0; s < ASTRIDE; s++) coef[s] = al[s];
-#pragma unroll 4
-          for (int i = pos + lane; i < kend; i += 32) {
-            const int e = i + shift;
-            T c[Rec::n];
-            Rec::load(rec, e, c);
-            T val;
-            if constexpr (FAITHFUL) {
-              val = c[1] * coef[0];
-            } else {
-              val = T(0);
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
+            T c[kStream][Rec::n];
+            unsigned ix[kStream];
 #pragma unroll
-              for (int s = 0; s < Rec::n; s++) val += c[s] * coef[s];
+            for (int u = 0; u < kStream; u++) {
+              const int e = min(i0 + 32 * u, kend - 1) + shift;
+              ix[u] = ridx[e];
+              Rec::load(rec, e, c[u]);
             }
-            atomicAdd(&U[ridx[e] >> 16], val);
+#pragma unroll
+            for (int u = 0; u < kStream; u++) {
+              T val;
+              if constexpr (FAITHFUL) {
+                val = c[u][1] * coef[0];
+              } else {
+                val = T(0);
+#pragma unroll
+                for (int s = 0; s < Rec::n; s++) val += c[u][s] * coef[s];
+              }
+              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u] >> 16], val);
+            }
           }
           pos = kend;
           k++;
@@ -614,10 +735,30 @@ __global__ void __launch_bounds__(sizeof(T) == 8 ? 512 : 1024, 1)
       // ---- pass 2: w = U - a_k v_k, P <- w, U <- v_k, b_k = ||w|| ----
       const T ta = T(a);
       T b_acc = T(0);
-      if (xin) {
+      if constexpr (PAIRED) {
+        if (pact) {
+          float2 *P2 = reinterpret_cast<float2 *>(P);
+          float2 *U2 = reinterpret_cast<float2 *>(U);
+          const int PS2 = PS >> 1, US2 = US >> 1;
+          const int rowP2 = (OFF + py * pitch + pxc) >> 1;
+          const int rowU2 = (py * upitch + pxc) >> 1;
+          for (int z = zb; z < ze; z++) {
+            const float2 pv = P2[rowP2 + z * PS2];
+            const float2 uv = U2[rowU2 + z * US2];
+            float2 vk, w;
+            vk.x = pv.x * inv;
+            vk.y = phi ? pv.y * inv : 0.f;
+            w.x = uv.x - ta * vk.x;
+            w.y = phi ? uv.y - ta * vk.y : 0.f;
+            P2[rowP2 + z * PS2] = w;
+            U2[rowU2 + z * US2] = vk;
+            b_acc += w.x * w.x + w.y * w.y;
+          }
+        }
+      } else if (xin) {
         for (int y = y_begin; y < y_end; y++) {
           const int rowP = OFF + y * pitch + x;
-          const int rowU = y * nx + x;
+          const int rowU = y * upitch + x;
           for (int z = 0; z < nz; z++) {
             const T pv = P[rowP + z * PS];
             const T vk = pv * inv;

@@ -9,7 +9,7 @@
 
 namespace sq {
 
-constexpr int kMaxWarpsF32 = 32;  // one CTA per SM, up to 32 warps (64 registers/thread)
+constexpr int kMaxWarpsF32 = 16;  // one CTA per SM, 16 warps: 128 registers/thread
 constexpr int kMaxWarpsF64 = 16;  // FP64 register window needs up to 128 registers/thread
 
 // device status bits (ORed by the kernels)
