@@ -145,6 +145,21 @@ sq_status sq_last_kernel_times(sq_handle *h, double *ms);
  * chain on every SM; the peak against which the FP32 Lanczos kernel is reported. */
 sq_status sq_measure_fp32_peak(int device, double *tflops);
 
+/* Allocation-free form of sq_fermi_density_energy_device; no counterpart in the reference.
+ * For callers that must not allocate device memory (a host framework that owns the device
+ * allocator, a fixed memory budget, or a stream-ordered pipeline that cannot afford the
+ * allocator's implicit synchronisation): no handle, no cudaMalloc/cudaFree; the kernel runs
+ * on a static scratch array of the library (about 410 KiB per GPU, held until exit).
+ * DEVICE inputs d_lambda, d_weights [n_nodes][n_qp]; d_rho [n_nodes] may be NULL; the
+ * HOST array out[3] receives lambda_f, e_band and ts; maxit <= 200 (else SQ_CAPACITY).
+ * The first call on a device looks up the array's address, so make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.  Synchronises
+ * `stream` before returning. */
+sq_status sq_fermi_density_energy_noalloc(const double *d_lambda, const double *d_weights,
+                                          long n_nodes, int n_qp, double beta,
+                                          double n_electrons, double dV, double tol, int maxit,
+                                          double *d_rho, double *out, void *stream);
+
 /* Message of the last failing call on this thread. */
 const char *sq_last_error_string(void);
 

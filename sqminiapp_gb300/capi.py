@@ -47,6 +47,8 @@ SIGNATURES = {
     "sq_fermi_density_energy_device": (ctypes.c_int, [_vp, _vp, _vp, _l, _d, _d, _dp, _vp, _dp,
                                                       _dp, _vp]),
     "sq_last_kernel_times": (ctypes.c_int, [_vp, _dp]),
+    "sq_fermi_density_energy_noalloc": (ctypes.c_int, [_vp, _vp, _l, ctypes.c_int, _d, _d, _d,
+                                                       _d, ctypes.c_int, _vp, _dp, _vp]),
     "sq_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int, _dp]),
     "sq_last_error_string": (ctypes.c_char_p, []),
 }

@@ -24,6 +24,14 @@ sq_status fail(sq_status s, const std::string &msg) {
   return s;
 }
 
+}  // namespace
+
+namespace sq {
+void set_noalloc_error(const std::string &msg) { g_last_error = msg; }
+}  // namespace sq
+
+namespace {
+
 struct CudaError : std::runtime_error {
   explicit CudaError(const std::string &m) : std::runtime_error(m) {}
 };

@@ -15,6 +15,11 @@
 // kStatusTimeout instead of waiting forever.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "sq_gb300.h"
 #include "sq_kernels.hpp"
 
 namespace sq {
@@ -194,6 +199,9 @@ __global__ void __launch_bounds__(kFermiBlock)
 
 }  // namespace
 
+// The message of sq_fermi_density_energy_noalloc failures, reported by sq_last_error_string.
+void set_noalloc_error(const std::string &msg);
+
 size_t fermi_scratch_doubles(int grid, int maxit) { return (size_t)grid * (maxit + 4); }
 
 cudaError_t launch_fermi(const double *lambda, const double *w, long long n_nodes, int nqp,
@@ -208,6 +216,123 @@ cudaError_t launch_fermi(const double *lambda, const double *w, long long n_node
                   (void *)&barrier, (void *)&status};
   return cudaLaunchCooperativeKernel((const void *)fermi_kernel, dim3(grid), dim3(kFermiBlock),
                                      args, 0, s);
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free entry point.
+//
+// Some callers cannot call cudaMalloc: code running inside a host framework that owns the
+// device allocator and forbids side allocations, plugin hosts that run with a fixed memory
+// budget, and stream-ordered pipelines that must not hit the allocator's implicit device
+// synchronisation between steps.  For them the Fermi-level kernel can run on a file-scope
+// scratch array that is part of the loaded module instead of on handle-owned buffers.
+//
+// Scratch capacity: kNoallocMaxBlocks CTA partials for each of kNoallocMaxIters bisection
+// steps plus four rows for the bracket and energy sums (about 410 KiB of doubles), the grid
+// barrier, the four scalar results and a status word.  Every GPU that loads the library
+// holds this array until the process exits.  All calls share it and it keeps the contents
+// of the last call: the barrier and the status word are cleared at the start of each call,
+// everything else is written before it is read.  Two calls whose work overlaps on the GPU
+// (on different streams, or from different host threads) race on the array and give wrong
+// results; calls must be ordered.
+// ---------------------------------------------------------------------------------------
+namespace {
+constexpr int kNoallocMaxBlocks = 256;
+constexpr int kNoallocMaxIters = 200;
+constexpr size_t kNoallocPartials = (size_t)kNoallocMaxBlocks * (kNoallocMaxIters + 4);
+
+struct NoallocScratch {
+  double partials[kNoallocPartials];
+  double out[4];
+  unsigned barrier[2];
+  int status;
+  int pad;
+};
+
+static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+NoallocScratch *g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+extern "C" sq_status sq_fermi_density_energy_noalloc(const double *d_lambda,
+                                                     const double *d_weights, long n_nodes,
+                                                     int n_qp, double beta, double n_electrons,
+                                                     double dV, double tol, int maxit,
+                                                     double *d_rho, double *out, void *stream) {
+  if (!d_lambda || !d_weights || !out) {
+    set_noalloc_error("null argument");
+    return SQ_BAD_INPUT;
+  }
+  if (n_nodes <= 0 || n_qp <= 0 || !(beta > 0) || !(dV > 0) || !(tol > 0)) {
+    set_noalloc_error("n_nodes, n_qp, beta, dV and tol must be positive");
+    return SQ_BAD_INPUT;
+  }
+  if (maxit < 1 || maxit > kNoallocMaxIters) {
+    set_noalloc_error("maxit must be 1.." + std::to_string(kNoallocMaxIters) +
+                      " (capacity of the static scratch array)");
+    return SQ_CAPACITY;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    set_noalloc_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return SQ_CUDA_ERROR;
+  }
+  // set-up, once per device, with that device current: resolve the array's device address
+  NoallocScratch *scr = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void *ptr = nullptr;
+      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        set_noalloc_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        return SQ_CUDA_ERROR;
+      }
+      g_noalloc_ptr[dev] = reinterpret_cast<NoallocScratch *>(ptr);
+    }
+    scr = g_noalloc_ptr[dev];
+  }
+  int sms = 0, per_sm = 0;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+      (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fermi_kernel, kFermiBlock, 0)) !=
+          cudaSuccess) {
+    set_noalloc_error(std::string("device query: ") + cudaGetErrorString(e));
+    return SQ_CUDA_ERROR;
+  }
+  if (per_sm < 1) {
+    set_noalloc_error("the Fermi kernel cannot be resident on this device");
+    return SQ_CUDA_ERROR;
+  }
+  // one CTA per SM (co-resident for the cooperative launch), as the handle-based path uses
+  const int grid = std::min(sms, kNoallocMaxBlocks);
+  cudaStream_t s = (cudaStream_t)stream;
+  if ((e = cudaMemsetAsync(&scr->status, 0, sizeof(int), s)) != cudaSuccess ||
+      (e = launch_fermi(d_lambda, d_weights, n_nodes, n_qp, beta, n_electrons, dV, tol, maxit,
+                        d_rho, scr->out, scr->partials, scr->barrier, &scr->status, grid, s)) !=
+          cudaSuccess) {
+    set_noalloc_error(std::string("fermi kernel: ") + cudaGetErrorString(e));
+    return SQ_CUDA_ERROR;
+  }
+  double res[4];
+  int st = 0;
+  if ((e = cudaMemcpyAsync(res, scr->out, sizeof(res), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(&st, &scr->status, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess) {
+    set_noalloc_error(std::string("result copy: ") + cudaGetErrorString(e));
+    return SQ_CUDA_ERROR;
+  }
+  if (st & kStatusTimeout) {
+    set_noalloc_error("a device-side wait gave up");
+    return SQ_DEVICE_TIMEOUT;
+  }
+  out[0] = res[0];
+  out[1] = res[1];
+  out[2] = res[2];
+  return SQ_OK;
 }
 
 }  // namespace sq
