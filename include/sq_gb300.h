@@ -137,6 +137,14 @@ sq_status sq_fermi_density_energy_device(sq_handle *h, const double *d_lambda,
                                          double *d_rho, double *e_band, double *ts,
                                          void *stream);
 
+/* Electron count N_e(lambda_f) = 2 sum_nodes sum_q w f(lambda - lambda_f) over DEVICE buffers
+ * [n_nodes][n_qp], returned to host memory: the constraint function the reference declares as
+ * constraint_lssgq (src/lsdft.h:98).  One scalar per call: the local term of a Fermi
+ * bisection whose nodes are sharded over several GPUs (sum over ranks, then bisect).
+ * Synchronises `stream`. */
+sq_status sq_electron_count_device(sq_handle *h, const double *d_lambda, const double *d_weights,
+                                   long n_nodes, double lambda_f, double *count, void *stream);
+
 /* Device time (ms) of the kernels of the last nodes_and_weights call, measured with CUDA
  * events on the stream they ran on: ms[0] Lanczos kernel, ms[1] quadrature kernel. */
 sq_status sq_last_kernel_times(sq_handle *h, double *ms);

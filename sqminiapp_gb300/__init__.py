@@ -164,6 +164,16 @@ class LSDFT:
               "sq_fermi_density_energy")
         return {"lambda_f": lf.value, "rho": rho, "e_band": eb.value, "ts": ts.value}
 
+    def electron_count_device(self, d_lambda, d_weights, n_nodes, lambda_f, stream=0):
+        """N_e(lambda_f) of device quadrature arrays (constraint_lssgq, src/lsdft.h:98)."""
+        c = ctypes.c_double()
+        check(self._lib.sq_electron_count_device(self._h, ctypes.c_void_p(d_lambda),
+                                                 ctypes.c_void_p(d_weights), int(n_nodes),
+                                                 float(lambda_f), ctypes.byref(c),
+                                                 ctypes.c_void_p(stream)),
+              "sq_electron_count_device")
+        return c.value
+
     def fermi_density_energy_device(self, d_lambda, d_weights, n_nodes, n_electrons, tol,
                                     d_rho, stream=0):
         lf = ctypes.c_double()

@@ -46,6 +46,7 @@ SIGNATURES = {
     "sq_fermi_density_energy": (ctypes.c_int, [_vp, _dp, _dp, _l, _d, _d, _dp, _dp, _dp, _dp]),
     "sq_fermi_density_energy_device": (ctypes.c_int, [_vp, _vp, _vp, _l, _d, _d, _dp, _vp, _dp,
                                                       _dp, _vp]),
+    "sq_electron_count_device": (ctypes.c_int, [_vp, _vp, _vp, _l, _d, _dp, _vp]),
     "sq_last_kernel_times": (ctypes.c_int, [_vp, _dp]),
     "sq_fermi_density_energy_noalloc": (ctypes.c_int, [_vp, _vp, _l, ctypes.c_int, _d, _d, _d,
                                                        _d, ctypes.c_int, _vp, _dp, _vp]),

@@ -614,6 +614,24 @@ sq_status sq_fermi_density_energy(sq_handle *h, const double *lambda, const doub
   });
 }
 
+sq_status sq_electron_count_device(sq_handle *h, const double *d_lambda, const double *d_weights,
+                                   long n_nodes, double lambda_f, double *count, void *stream) {
+  if (!h || !d_lambda || !d_weights || !count) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    if (n_nodes <= 0) return fail(SQ_BAD_INPUT, "n_nodes must be positive");
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int grid = 4 * h->num_sms;  // <= fermi scratch rows (maxit + 4) * fermi_grid
+    double *partial = h->d_fermi_scratch, *out = h->d_fermi_out;
+    ck(sq::launch_electron_count(d_lambda, d_weights, n_nodes, h->lp.nqp, h->info.beta, lambda_f,
+                                 partial, grid, out, s),
+       "electron count");
+    ck(cudaMemcpyAsync(count, out, sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    return SQ_OK;
+  });
+}
+
 sq_status sq_last_kernel_times(sq_handle *h, double *ms) {
   if (!h || !ms) return fail(SQ_BAD_INPUT, "null argument");
   return guarded([&] {

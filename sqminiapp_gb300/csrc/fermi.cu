@@ -197,7 +197,48 @@ __global__ void __launch_bounds__(kFermiBlock)
   }
 }
 
+constexpr int kCountBlock = 256;
+
+// Partial electron counts: one per CTA, in a fixed grid-stride order.
+__global__ void __launch_bounds__(kCountBlock)
+    count_partials_kernel(const double *__restrict__ lambda, const double *__restrict__ w,
+                          long long n, double beta, double lf, double *__restrict__ partial) {
+  __shared__ double red[kCountBlock / 32];
+  double c = 0.0;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n;
+       e += (long long)gridDim.x * blockDim.x)
+    c += 2.0 * w[e] * fermi_dirac(beta, lambda[e], lf);
+  c = warp_sum_d(c);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < kCountBlock / 32; i++) t += red[i];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void sum_partials_kernel(const double *__restrict__ partial, int n,
+                                    double *__restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < n; i++) t += partial[i];
+    *out = t;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_electron_count(const double *lambda, const double *w, long long n_nodes,
+                                  int nqp, double beta, double lf, double *partial, int grid,
+                                  double *out, cudaStream_t s) {
+  const long long n = n_nodes * nqp;
+  count_partials_kernel<<<grid, kCountBlock, 0, s>>>(lambda, w, n, beta, lf, partial);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_partials_kernel<<<1, 32, 0, s>>>(partial, grid, out);
+  return cudaGetLastError();
+}
 
 // The message of sq_fermi_density_energy_noalloc failures, reported by sq_last_error_string.
 void set_noalloc_error(const std::string &msg);

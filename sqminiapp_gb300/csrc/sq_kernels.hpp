@@ -47,6 +47,11 @@ cudaError_t launch_fermi(const double *lambda, const double *w, long long n_node
                          double *rho, double *out, double *scratch, unsigned *barrier,
                          int *status, int grid, cudaStream_t s);
 
+// N_e(lf) = 2 sum w f(lambda - lf) over n_nodes*nqp entries; `partial` holds `grid` doubles.
+cudaError_t launch_electron_count(const double *lambda, const double *w, long long n_nodes,
+                                  int nqp, double beta, double lf, double *partial, int grid,
+                                  double *out, cudaStream_t s);
+
 // FP32 FMA throughput of `device` in TFLOP/s (register-resident FMA chains on every SM).
 cudaError_t measure_fp32_peak(int device, double *tflops);
 
