@@ -252,13 +252,12 @@ def run_ours(args):
     peak = np.zeros(1)
     check(lib().sq_measure_fp32_peak(local, peak.ctypes.data_as(
         __import__("ctypes").POINTER(__import__("ctypes").c_double))), "fp32 peak")
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "lanczos_traffic.json")
+    traffic = None  # DRAM bytes per launch from the committed ncu summary, if it covers this workload
+    tp = os.path.join(ROOT, "profiles", "lanczos_traffic.txt")
     if os.path.exists(tp):
-        with open(tp) as f:
-            tj = json.load(f)
-        if tj.get("workload") == args.config:
-            traffic = tj.get("bytes_per_launch")
+        kv = dict(line.split(":", 1) for line in open(tp) if ":" in line and not line.startswith("#"))
+        if kv.get("workload", "").strip() == args.config and args.max_nodes == 0:
+            traffic = float(kv["bytes_per_launch"])
 
     # e2e through the host-buffer API
     e2e = None
