@@ -558,29 +558,6 @@ __global__ void __launch_bounds__(512, 1)
           k++;
         }
       }
-      __syncthreads();
-
-      // ---- projector coefficients alpha from the gathered c, plus <v, V_nl v> ----
-      double a_part = 0.0;
-      for (int e = threadIdx.x; e < n_slot * ASTRIDE; e += blockDim.x) {
-        if constexpr (FAITHFUL) {
-          const double cg = (double)cacc[2 * e] * (double)inv;
-          const double cs = (double)cacc[2 * e + 1] * (double)inv;
-          cacc[2 * e] = T(0);
-          cacc[2 * e + 1] = T(0);
-          alpha[e] = T(cg);
-          a_part += cs * cg;
-        } else {
-          const int sl = e / NLM, r = e - sl * NLM;
-          const TypeDesc &td = p.types[slot_type[sl]];
-          const int l = p.rank_l[r];
-          const double c = (double)cacc[e] * (double)inv;
-          cacc[e] = T(0);
-          const double gl = (td.chan_mask & (1 << l)) ? td.gamma[l] : 0.0;
-          alpha[e] = T(gl * c);
-          a_part += gl * c * c;
-        }
-      }
 
       // ---- pass 1: stencil + Veff, U <- H v_k - b_{k-1} U, a_k partial ----
       T a_acc = T(0);
@@ -692,6 +669,32 @@ __global__ void __launch_bounds__(512, 1)
           }
         }
       }
+      // the gather above and the stencil touch disjoint outputs (atom slots, U), so warps move
+      // from one to the other without waiting; one barrier then covers both
+      __syncthreads();
+
+      // ---- projector coefficients alpha from the gathered c, plus <v, V_nl v> ----
+      double a_part = 0.0;
+      for (int e = threadIdx.x; e < n_slot * ASTRIDE; e += blockDim.x) {
+        if constexpr (FAITHFUL) {
+          const double cg = (double)cacc[2 * e] * (double)inv;
+          const double cs = (double)cacc[2 * e + 1] * (double)inv;
+          cacc[2 * e] = T(0);
+          cacc[2 * e + 1] = T(0);
+          alpha[e] = T(cg);
+          a_part += cs * cg;
+        } else {
+          const int sl = e / NLM, r = e - sl * NLM;
+          const TypeDesc &td = p.types[slot_type[sl]];
+          const int l = p.rank_l[r];
+          const double c = (double)cacc[e] * (double)inv;
+          cacc[e] = T(0);
+          const double gl = (td.chan_mask & (1 << l)) ? td.gamma[l] : 0.0;
+          alpha[e] = T(gl * c);
+          a_part += gl * c * c;
+        }
+      }
+
       __syncthreads();
 
       // ---- nonlocal scatter: U += sum_lm chi_lm alpha_lm over this warp's range ----
