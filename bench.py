@@ -17,6 +17,9 @@ roofline: the Lanczos kernel's algorithmic FP32 FLOPs per launch over its CUDA-e
          against the device's FP32 FMA peak measured by the library's probe kernel.
 cpu_baseline / --impl reference: the FP64 CPU restatement of the reference's per-node path
          (oracle/, one thread per host core) on a bounded sample of the same workload.
+scf:     time-to-SCF-convergence (the second half of the headline metric) of the FP32 and the
+         FP64 engine on the 4-atom cell (h = 0.5, Rcut = 6, 30 Lanczos steps), from the
+         atomic-superposition density, with their free energies per atom.
 
 Multi-GPU (torchrun): one rank per GPU, each rank an independent cell (seed + rank), no
 collective on the data path (weak scaling); max time over ranks.
@@ -37,6 +40,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD = "mg32_h0.5_rc6.5_q40"
+SCF_WORKLOAD = "mg4_h0.5_rc6_q30"
 METRIC = "node-Lanczos/s"
 
 
@@ -53,6 +57,10 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--max-nodes", type=int, default=0,
                    help="process only the first N nodes per step (profiling of small cases)")
+    p.add_argument("--scf-config", default=SCF_WORKLOAD,
+                   help="cell of the time-to-SCF leg ('none' skips it)")
+    p.add_argument("--scf-precisions", default="32,64",
+                   help="engines timed by the time-to-SCF leg")
     return p.parse_args()
 
 
@@ -290,6 +298,10 @@ def run_ours(args):
         cpu = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
                "sample": sample + "; FP64 restatement of the reference path"}
 
+    scf = None
+    if rank == 0 and world == 1 and args.scf_config != "none":
+        scf = scf_leg(args, local)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
@@ -309,12 +321,40 @@ def run_ours(args):
                          "kernel_ms": lz_ms, "flops_per_launch": flops,
                          "peak_kind": "measured FP32 FMA probe"},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 4 * args.steps,
-            "clocks": clk, "wall_s": t_wall,
+            "clocks": clk, "wall_s": t_wall, "scf": scf,
         }
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+def scf_leg(args, local):
+    """Time-to-SCF-convergence of the FP32 and FP64 engines on one cell (host wall clock of
+    sq_scf_run from the atomic-superposition start; engine setup timed apart)."""
+    from sqminiapp_gb300 import LSDFT
+    (deck_dir, name, meta), cfg = make_deck(args.scf_config, 0)
+    out = {"workload": args.scf_config, "atoms": meta["natoms"], "start": "atomic superposition",
+           "stop": "relative density residual < TOL_SCF (1e-6; 3e-5 floor for FP32 vectors)"}
+    for prec in [int(p) for p in args.scf_precisions.split(",") if p]:
+        t0 = time.perf_counter()
+        eng = LSDFT(deck_dir, name, faithful=False, precision=prec, device=local)
+        eng.scf_begin()  # builds the pseudocharges / Poisson symbol once per geometry
+        setup_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r = eng.SCF_LSSGQ(raise_on_maxit=False)
+        wall = time.perf_counter() - t0
+        out["fp%d" % prec] = {"seconds": wall, "setup_seconds": setup_s,
+                              "iterations": r["iterations"], "converged": bool(r["converged"]),
+                              "free_energy_per_atom": r["free_energy_per_atom"],
+                              "residual": r["residual"], "tol": r["tol"],
+                              "sq_seconds": r["sq_ms"] / 1e3}
+        eng.close()
+    if "fp32" in out and "fp64" in out:
+        out["speedup_fp32_vs_fp64"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+        out["dF_per_atom_fp32_vs_fp64"] = abs(out["fp32"]["free_energy_per_atom"] -
+                                              out["fp64"]["free_energy_per_atom"])
+    return out
 
 
 def main():

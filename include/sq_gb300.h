@@ -168,6 +168,91 @@ sq_status sq_fermi_density_energy_noalloc(const double *d_lambda, const double *
                                           double n_electrons, double dV, double tol, int maxit,
                                           double *d_rho, double *out, void *stream);
 
+/* ---- SCF closure (periodic decks, BOUNDARY_CONDITION 2) ----
+ * The self-consistent loop that the reference declares as SCF_LSSGQ (src/lsdft.h:153) with
+ * SolvePoisson (:93), mix (:183), Vxc_Calc_CA_PW / Exc_Calc_CA_PW (:201-202) and
+ * SystemEnergy_Calc_lssgq (:209), none of which has a body in the reference.  One iteration:
+ * pseudocharge Poisson solve of the FD Laplacian (exact, in Fourier space), LDA
+ * (Slater + Perdew-Wang 92) potential, the per-node Lanczos/quadrature pass with that Veff,
+ * Fermi bisection, density residual, Harris-Foulkes free energy and Periodic-Pulay mixing
+ * (MIXING_PARAMETER / MIXING_HISTORY / PULAY_FREQUENCY, src/lsdft_readfiles.cc:219-228). */
+typedef struct sq_scf_options {
+  double tol;               /* ||rho_out - rho_in|| / ||rho_out|| target; <= 0: TOL_SCF;
+                               raised to 3e-5 for an FP32 engine */
+  int maxit;                /* <= 0: MAXIT_SCF */
+  double mixing_parameter;  /* <= 0: MIXING_PARAMETER */
+  int mixing_history;       /* <= 0: MIXING_HISTORY (at most 16) */
+  int pulay_frequency;      /* <= 0: PULAY_FREQUENCY */
+  double fermi_tol;         /* bisection tolerance on lambda_f; <= 0: 1e-12 */
+  double kerker_ktf;        /* Kerker preconditioner k_TF (1/bohr) of the mixing: > 0 that value,
+                               0 the default 1.0 (the reference mixes preconditioned,
+                               src/lsdft_readfiles.cc:102), < 0 no preconditioner */
+} sq_scf_options;
+
+typedef struct sq_scf_result {
+  int iterations;          /* SCF iterations done since sq_scf_begin */
+  int converged;           /* 1 once the residual is below tol */
+  double free_energy;      /* Ha: e_band + e_xc - e_xc_dc + e_electrostatic - e_self + e_corr + ts */
+  double free_energy_per_atom;
+  double e_band;           /* 2 sum w lambda f */
+  double e_xc;             /* int rho_in eps_xc(rho_in) */
+  double e_xc_dc;          /* int rho_in Vxc(rho_in) */
+  double e_electrostatic;  /* 1/2 int (b - rho_in) phi */
+  double e_self;           /* 1/2 sum_J int b_J V_J */
+  double e_corr;           /* overlap correction of the pseudocharges */
+  double ts;               /* -TS = (2/beta) sum w [f ln f + (1-f) ln(1-f)] */
+  double lambda_f;         /* Fermi level */
+  double residual;         /* ||rho_out - rho_in|| / ||rho_out|| of the last iteration */
+  double seconds;          /* host wall time of the iterations since sq_scf_begin */
+  double sq_ms;            /* device time of the Lanczos + quadrature kernels, summed */
+  double tol;              /* residual target in force: the requested one, but at least 3e-5
+                              with FP32 Lanczos vectors (their residual noise floor is ~1e-5) */
+} sq_scf_result;
+
+/* Start an SCF: rho_init HOST [n_nodes] (NULL = superposition of the psd atomic valence
+ * densities, SuperposAtRho of src/ilsdft.h:269), cut at zero and scaled to the electron
+ * count.  opt may be NULL (deck values).  Clears the mixing history. */
+sq_status sq_scf_begin(sq_handle *h, const sq_scf_options *opt, const double *rho_init);
+/* The same with a DEVICE initial density (a learned or checkpointed guess). */
+sq_status sq_scf_begin_device(sq_handle *h, const sq_scf_options *opt, const double *d_rho_init);
+/* One SCF iteration; result (may be NULL) receives the state after it. */
+sq_status sq_scf_step(sq_handle *h, sq_scf_result *result);
+/* sq_scf_begin, then iterate until converged (SQ_OK) or MAXIT_SCF (SQ_NO_CONVERGENCE). */
+sq_status sq_scf_run(sq_handle *h, const sq_scf_options *opt, const double *rho_init,
+                     sq_scf_result *result);
+/* HOST copies [n_nodes] of the last output density and of the next input density (either
+ * may be NULL). */
+sq_status sq_scf_get_density(sq_handle *h, double *rho_out, double *rho_in);
+/* HOST copies [n_nodes] of the pseudocharge b, the initial density, and the phi / Vxc of the
+ * last iteration (any may be NULL); scalars[4] = E_self, E_self of the reference
+ * pseudocharges, E_c, int b. */
+sq_status sq_scf_get_fields(sq_handle *h, double *b, double *rho0, double *phi, double *vxc,
+                            double *scalars);
+/* Free energy and residual of every iteration since sq_scf_begin (up to cap entries). */
+sq_status sq_scf_history(sq_handle *h, int cap, double *free_energy, double *residual, int *count);
+/* Host evaluation of the LDA functional the SCF uses: eps_xc and Vxc per density value. */
+sq_status sq_lda_pw92(const double *rho, long n, double *eps, double *v);
+
+/* ---- The reference's text files (one block of the grid per rank; one GPU: corner 0, dims =
+ * FD_GRID).  Files are "<prefix>_<rank>.den" / ".lambdas"; reading fails with SQ_BAD_INPUT
+ * when the header's block differs from corner/dims. */
+/* Print_ElecDens (src/lsdft_readfiles.cc:1106-1138): header "xcor ycor zcor lx ly lz", then
+ * "k j i value" (%0.16lf) per point; rho is HOST [dims[2]][dims[1]][dims[0]]. */
+sq_status sq_write_density_file(const char *prefix, int rank, const int corner[3],
+                                const int dims[3], const double *rho);
+/* Read_ElecDens (:1242-1289): the inverse; a density to restart an SCF from. */
+sq_status sq_read_density_file(const char *prefix, int rank, const int corner[3],
+                               const int dims[3], double *rho);
+/* Print_MinMaxLambda / Read_MinMaxLambda (:1294-1381): "LIpos lambda_min lambda_max". */
+sq_status sq_write_lambda_file(const char *prefix, int rank, const int corner[3],
+                               const int dims[3], const double *lambda_min,
+                               const double *lambda_max);
+sq_status sq_read_lambda_file(const char *prefix, int rank, const int corner[3],
+                              const int dims[3], double *lambda_min, double *lambda_max);
+/* The input-parameter and initialization echo of the reference's .out file
+ * (src/lsdft_readfiles.cc:520-607) for the keywords this engine reads. */
+sq_status sq_write_output_echo(const sq_handle *h, const char *path);
+
 /* Message of the last failing call on this thread. */
 const char *sq_last_error_string(void);
 

@@ -58,6 +58,8 @@ def lib():
                                                ctypes.c_double, ctypes.c_int, _dp, _dp, _dp, _dp,
                                                _ip]
         L.sqo_spline.argtypes = [_dp, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int]
+        L.sqo_psd_tables.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _dp, _dp, _dp]
+        L.sqo_atoms.argtypes = [ctypes.c_void_p, _dp, _ip]
         L.sqo_ylm.restype = ctypes.c_double
         L.sqo_ylm.argtypes = [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_int]
         _lib = L
@@ -122,6 +124,22 @@ class Oracle:
         c = np.zeros(3 * self.ntype)
         lib().sqo_pseudocharge_cutoff(self._h, _d(c))
         return c.reshape(self.ntype, 3)
+
+    def psd_tables(self, t=0):
+        """(r, V_loc, rho_atom, z_valence) of type t as read from its psd file."""
+        n = ctypes.c_int(0)
+        lib().sqo_psd_tables(self._h, t, ctypes.byref(n), None, None, None, None)
+        r, v, rho = np.zeros(n.value), np.zeros(n.value), np.zeros(n.value)
+        z = ctypes.c_double(0)
+        lib().sqo_psd_tables(self._h, t, ctypes.byref(n), _d(r), _d(v), _d(rho), ctypes.byref(z))
+        return r, v, rho, z.value
+
+    def atoms(self):
+        """(positions [natoms, 3], types [natoms]) in .ion order."""
+        pos = np.zeros((self.natoms, 3))
+        typ = np.zeros(self.natoms, np.int32)
+        lib().sqo_atoms(self._h, _d(pos), typ.ctypes.data_as(_ip))
+        return pos, typ
 
     def local_overlap_count(self, cor, dims, extra_xyz=None):
         cnt = ctypes.c_int(0)

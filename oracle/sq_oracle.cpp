@@ -914,6 +914,30 @@ int sqo_pseudocharge_cutoff(void *h, double *out) {
   return 0;
 }
 
+int sqo_psd_tables(void *h, int type, int *n, double *r, double *vloc, double *rho_atom,
+                   double *zval) {
+  System &S = *(System *)h;
+  if (type < 0 || type >= S.d.ntype) return 1;
+  const Psd &p = S.psd[type];
+  *n = p.size;
+  for (int i = 0; i < p.size; i++) {
+    if (r) r[i] = p.r[i];
+    if (vloc) vloc[i] = p.Vloc[i];
+    if (rho_atom) rho_atom[i] = p.uu[i];
+  }
+  if (zval) *zval = S.d.noe[type];
+  return 0;
+}
+
+int sqo_atoms(void *h, double *pos, int *types) {
+  System &S = *(System *)h;
+  for (int n = 0; n < S.d.natoms; n++) {
+    for (int a = 0; a < 3; a++) pos[3 * n + a] = S.d.pos[3 * n + a];
+    types[n] = S.d.type_of[n];
+  }
+  return 0;
+}
+
 // GetInfluencingAtoms_Local: src/lsdft_initObjs.cc:1409-1665
 int sqo_local_overlap_count(void *h, int xcor, int ycor, int zcor, int lx, int ly, int lz,
                             const double *extra_xyz, int *count) {

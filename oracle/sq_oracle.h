@@ -46,6 +46,14 @@ int sqo_gamma(void *h, int type, double *gamma4);
 /* Pseudocharge cutoff (x,y,z) of every type: out[3*ntype]. */
 int sqo_pseudocharge_cutoff(void *h, double *out);
 
+/* Radial tables of type t as read from its psd file (r, V_loc, valence density
+ * rho_atom = value / (4 pi r^2); each *n entries, any may be NULL) and its valence charge. */
+int sqo_psd_tables(void *h, int type, int *n, double *r, double *vloc, double *rho_atom,
+                   double *zval);
+
+/* Atom positions pos[natoms][3] and types[natoms] in .ion order. */
+int sqo_atoms(void *h, double *pos, int *types);
+
 /* Number of (atom, periodic image) pairs whose pseudocharge box overlaps the
  * block [xcor,xcor+lx) x [ycor,..) x [zcor,..) (GetInfluencingAtoms_Local).
  * If extra_xyz is not NULL an additional atom at that position is included,

@@ -12,15 +12,18 @@ Names follow the reference (SQMiniApp ``src/lsdft.h``):
 * ``LSDFT.NodesAndWeights_LSSGQ``   -- src/lsdft_scf.cc:32-82 (per-node Lanczos + quadrature)
 * ``LSDFT.CalculateDensity_lssgq``  -- declared at src/lsdft.h:100 (Fermi bisection, density,
                                        band energy), implemented from the SQ method
+* ``LSDFT.SCF_LSSGQ``               -- declared at src/lsdft.h:153 (the SCF loop: Poisson,
+                                       LDA, SQ pass, Fermi level, energy, Periodic Pulay)
 """
 import ctypes
 import os
 
 import numpy as np
 
-from .capi import SQ_OK, SqError, SqInfo, SqOptions, lib, check, library_path
+from .capi import SQ_OK, SqError, SqInfo, SqOptions, SqScfOptions, SqScfResult, lib, check, library_path
 
-__all__ = ["LSDFT", "SqError", "library_path", "DECK_DIR"]
+__all__ = ["LSDFT", "SqError", "library_path", "DECK_DIR", "lda_pw92", "Print_ElecDens",
+           "Read_ElecDens", "Print_MinMaxLambda", "Read_MinMaxLambda"]
 
 DECK_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "decks")
 
@@ -185,3 +188,141 @@ class LSDFT:
             ctypes.c_void_p(d_rho) if d_rho else None, ctypes.byref(eb), ctypes.byref(ts),
             ctypes.c_void_p(stream)), "sq_fermi_density_energy_device")
         return {"lambda_f": lf.value, "e_band": eb.value, "ts": ts.value}
+
+    # --- SCF closure (SCF_LSSGQ, src/lsdft.h:153) -----------------------------------------
+    @staticmethod
+    def _scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency, fermi_tol,
+                     kerker_ktf=None):
+        return SqScfOptions(float(tol or 0.0), int(maxit or 0), float(mixing_parameter or 0.0),
+                            int(mixing_history or 0), int(pulay_frequency or 0),
+                            float(fermi_tol or 0.0), float(kerker_ktf or 0.0))
+
+    def SCF_LSSGQ(self, rho_init=None, tol=None, maxit=None, mixing_parameter=None,
+                  mixing_history=None, pulay_frequency=None, fermi_tol=None, kerker_ktf=None,
+                  raise_on_maxit=True):
+        """Self-consistent field loop on the GPU until ||rho_out - rho_in|| / ||rho_out|| < tol.
+
+        rho_init: None (superposition of atomic valence densities) or a host density over the
+        FD grid.  None for any option takes the deck's value (TOL_SCF, MAXIT_SCF,
+        MIXING_PARAMETER, MIXING_HISTORY, PULAY_FREQUENCY); kerker_ktf None/0 = Kerker with
+        k_TF = 1/bohr, negative = unpreconditioned mixing.  Returns the result dict of the
+        last iteration with the per-iteration history of free energy and residual."""
+        opt = self._scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency,
+                                fermi_tol, kerker_ktf)
+        rp = None
+        if rho_init is not None:
+            rho_init = np.ascontiguousarray(rho_init, dtype=np.float64).reshape(-1)
+            if rho_init.size != self.n_nodes:
+                raise ValueError("rho_init must have one value per FD node")
+            rp = _ptr(rho_init)
+        res = SqScfResult()
+        st = self._lib.sq_scf_run(self._h, ctypes.byref(opt), rp, ctypes.byref(res))
+        if st != SQ_OK and not (st == 2 and not raise_on_maxit):
+            check(st, "sq_scf_run")
+        out = res.as_dict()
+        out["free_energy_history"], out["residual_history"] = self.scf_history()
+        return out
+
+    def scf_begin(self, rho_init=None, d_rho_init=None, **opts):
+        """Start an SCF by hand (then call scf_step); d_rho_init is a device address."""
+        opt = self._scf_options(opts.get("tol"), opts.get("maxit"), opts.get("mixing_parameter"),
+                                opts.get("mixing_history"), opts.get("pulay_frequency"),
+                                opts.get("fermi_tol"), opts.get("kerker_ktf"))
+        if d_rho_init is not None:
+            check(self._lib.sq_scf_begin_device(self._h, ctypes.byref(opt),
+                                                ctypes.c_void_p(d_rho_init)), "sq_scf_begin_device")
+            return
+        rp = None
+        if rho_init is not None:
+            rho_init = np.ascontiguousarray(rho_init, dtype=np.float64).reshape(-1)
+            rp = _ptr(rho_init)
+        check(self._lib.sq_scf_begin(self._h, ctypes.byref(opt), rp), "sq_scf_begin")
+
+    def scf_step(self):
+        res = SqScfResult()
+        check(self._lib.sq_scf_step(self._h, ctypes.byref(res)), "sq_scf_step")
+        return res.as_dict()
+
+    def scf_history(self):
+        n = ctypes.c_int()
+        check(self._lib.sq_scf_history(self._h, 0, None, None, ctypes.byref(n)), "sq_scf_history")
+        F = np.empty(n.value)
+        E = np.empty(n.value)
+        check(self._lib.sq_scf_history(self._h, n.value, _ptr(F), _ptr(E), ctypes.byref(n)),
+              "sq_scf_history")
+        return F, E
+
+    def scf_density(self):
+        """(rho_out of the last iteration, rho_in of the next one), host arrays."""
+        ro = np.empty(self.n_nodes)
+        ri = np.empty(self.n_nodes)
+        check(self._lib.sq_scf_get_density(self._h, _ptr(ro), _ptr(ri)), "sq_scf_get_density")
+        return ro, ri
+
+    def write_output_echo(self, path):
+        """The reference's .out header (input parameters, initialization) for this deck."""
+        check(self._lib.sq_write_output_echo(self._h, str(path).encode()), "sq_write_output_echo")
+
+    def scf_fields(self):
+        """Pseudocharge b, initial density, phi and Vxc of the last iteration, and the scalars
+        E_self, E_self(reference pseudocharges), E_c, int b."""
+        arrs = [np.empty(self.n_nodes) for _ in range(4)]
+        sc = np.empty(4)
+        check(self._lib.sq_scf_get_fields(self._h, *[_ptr(a) for a in arrs], _ptr(sc)),
+              "sq_scf_get_fields")
+        return {"b": arrs[0], "rho0": arrs[1], "phi": arrs[2], "vxc": arrs[3],
+                "e_self": sc[0], "e_self_ref": sc[1], "e_corr": sc[2], "b_total": sc[3]}
+
+
+def lda_pw92(rho):
+    """The library's host evaluation of the LDA functional: (eps_xc, Vxc) per density."""
+    rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+    e = np.empty_like(rho)
+    v = np.empty_like(rho)
+    check(lib().sq_lda_pw92(_ptr(rho), rho.size, _ptr(e), _ptr(v)), "sq_lda_pw92")
+    return e, v
+
+
+def _block(shape, corner):
+    nz, ny, nx = shape
+    c = (ctypes.c_int * 3)(*[int(v) for v in corner])
+    d = (ctypes.c_int * 3)(nx, ny, nz)
+    return c, d
+
+
+def Print_ElecDens(prefix, rho, rank=0, corner=(0, 0, 0)):
+    """Write rho [nz, ny, nx] (a rank's block) as <prefix>_<rank>.den in the reference format
+    (src/lsdft_readfiles.cc:1106-1138)."""
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    c, d = _block(rho.shape, corner)
+    check(lib().sq_write_density_file(str(prefix).encode(), int(rank), c, d, _ptr(rho)),
+          "sq_write_density_file")
+
+
+def Read_ElecDens(prefix, shape, rank=0, corner=(0, 0, 0)):
+    """Read <prefix>_<rank>.den (src/lsdft_readfiles.cc:1242-1289) into [nz, ny, nx]."""
+    rho = np.empty(shape)
+    c, d = _block(shape, corner)
+    check(lib().sq_read_density_file(str(prefix).encode(), int(rank), c, d, _ptr(rho)),
+          "sq_read_density_file")
+    return rho
+
+
+def Print_MinMaxLambda(prefix, lambda_min, lambda_max, shape, rank=0, corner=(0, 0, 0)):
+    """<prefix>_<rank>.lambdas (src/lsdft_readfiles.cc:1294-1328)."""
+    lo = np.ascontiguousarray(lambda_min, dtype=np.float64).reshape(-1)
+    hi = np.ascontiguousarray(lambda_max, dtype=np.float64).reshape(-1)
+    c, d = _block(shape, corner)
+    check(lib().sq_write_lambda_file(str(prefix).encode(), int(rank), c, d, _ptr(lo), _ptr(hi)),
+          "sq_write_lambda_file")
+
+
+def Read_MinMaxLambda(prefix, shape, rank=0, corner=(0, 0, 0)):
+    """Read <prefix>_<rank>.lambdas (src/lsdft_readfiles.cc:1333-1381)."""
+    n = int(np.prod(shape))
+    lo = np.empty(n)
+    hi = np.empty(n)
+    c, d = _block(shape, corner)
+    check(lib().sq_read_lambda_file(str(prefix).encode(), int(rank), c, d, _ptr(lo), _ptr(hi)),
+          "sq_read_lambda_file")
+    return lo, hi

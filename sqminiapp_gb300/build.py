@@ -14,6 +14,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libsq_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_LIB = "/usr/local/cuda/lib64"
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", CSRC,
           "-I", os.path.join(os.path.dirname(HERE), "include")]
 SOURCES = {
@@ -26,6 +27,9 @@ SOURCES = {
     "capi.cpp": ["-x", "cu"],
     "setup.cpp": [],
     "deck.cpp": [],
+    "scf_setup.cpp": [],
+    "scf.cu": [],
+    "io.cpp": [],
 }
 
 
@@ -62,7 +66,9 @@ def build(verbose=False):
             if log:
                 sys.stderr.write(log)
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcufft", "-lcudart_static", "-lrt", "-ldl", "-lpthread",
+                                                         "-Xlinker", "--no-undefined",
+                                                         "-Xlinker", "-rpath=" + CUDA_LIB]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

@@ -14,6 +14,7 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _vp = ctypes.c_void_p
 _l = ctypes.c_long
 _d = ctypes.c_double
+_ip = ctypes.POINTER(ctypes.c_int)
 
 
 class SqOptions(ctypes.Structure):
@@ -30,6 +31,23 @@ class SqInfo(ctypes.Structure):
                 ("rcut", ctypes.c_double), ("beta", ctypes.c_double), ("dV", ctypes.c_double),
                 ("n_electrons", ctypes.c_double), ("n_lm", ctypes.c_int),
                 ("proj_points_per_node", ctypes.c_double)]
+
+
+class SqScfOptions(ctypes.Structure):
+    _fields_ = [("tol", ctypes.c_double), ("maxit", ctypes.c_int),
+                ("mixing_parameter", ctypes.c_double), ("mixing_history", ctypes.c_int),
+                ("pulay_frequency", ctypes.c_int), ("fermi_tol", ctypes.c_double),
+                ("kerker_ktf", ctypes.c_double)]
+
+
+class SqScfResult(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("converged", ctypes.c_int)] + [
+        (n, ctypes.c_double) for n in ("free_energy", "free_energy_per_atom", "e_band", "e_xc",
+                                       "e_xc_dc", "e_electrostatic", "e_self", "e_corr", "ts",
+                                       "lambda_f", "residual", "seconds", "sq_ms", "tol")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 SIGNATURES = {
@@ -51,6 +69,20 @@ SIGNATURES = {
     "sq_fermi_density_energy_noalloc": (ctypes.c_int, [_vp, _vp, _l, ctypes.c_int, _d, _d, _d,
                                                        _d, ctypes.c_int, _vp, _dp, _vp]),
     "sq_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int, _dp]),
+    "sq_scf_begin": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _dp]),
+    "sq_scf_begin_device": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _vp]),
+    "sq_scf_step": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfResult)]),
+    "sq_scf_run": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _dp,
+                                  ctypes.POINTER(SqScfResult)]),
+    "sq_scf_get_density": (ctypes.c_int, [_vp, _dp, _dp]),
+    "sq_scf_get_fields": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp, _dp]),
+    "sq_scf_history": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, ctypes.POINTER(ctypes.c_int)]),
+    "sq_lda_pw92": (ctypes.c_int, [_dp, _l, _dp, _dp]),
+    "sq_write_density_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, _dp]),
+    "sq_read_density_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, _dp]),
+    "sq_write_lambda_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, _dp, _dp]),
+    "sq_read_lambda_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, _dp, _dp]),
+    "sq_write_output_echo": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "sq_last_error_string": (ctypes.c_char_p, []),
 }
 

@@ -11,106 +11,63 @@
 #include <stdexcept>
 #include <string>
 
+#include "handle.hpp"
 #include "sq_gb300.h"
 #include "sq_internal.hpp"
 #include "sq_kernels.hpp"
 
-namespace {
+namespace sq {
 
+namespace {
 thread_local std::string g_last_error;
+}  // namespace
 
 sq_status fail(sq_status s, const std::string &msg) {
   g_last_error = msg;
   return s;
 }
 
-}  // namespace
-
-namespace sq {
 void set_noalloc_error(const std::string &msg) { g_last_error = msg; }
-}  // namespace sq
 
-namespace {
-
-struct CudaError : std::runtime_error {
-  explicit CudaError(const std::string &m) : std::runtime_error(m) {}
-};
+const std::string &last_error() { return g_last_error; }
 
 void ck(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-template <typename P> void dev_alloc(P **ptr, size_t bytes, const char *what) {
-  *ptr = nullptr;
-  if (bytes == 0) bytes = 16;
-  ck(cudaMalloc((void **)ptr, bytes), what);
+void ensure_capacity(double *&ptr, long long &cap, long long need, const char *what) {
+  if (need <= cap) return;
+  dev_free(ptr);
+  dev_alloc(&ptr, sizeof(double) * (size_t)need, what);
+  cap = need;
 }
 
-template <typename P> void dev_free(P *&ptr) {
-  if (ptr) cudaFree((void *)ptr);
-  ptr = nullptr;
+}  // namespace sq
+
+using namespace sq;
+
+sq_handle::~sq_handle() {
+  sq::scf_destroy(scf);
+  dev_free(d_images);
+  dev_free(d_tables);
+  dev_free(d_veff_ext);
+  dev_free(d_veff_in);
+  dev_free(d_u);
+  dev_free(d_proj);
+  dev_free(d_status);
+  dev_free(d_ab);
+  dev_free(d_lambda);
+  dev_free(d_w);
+  dev_free(d_lmin);
+  dev_free(d_lmax);
+  dev_free(d_rho);
+  dev_free(d_fermi_scratch);
+  dev_free(d_bar);
+  dev_free(d_fermi_out);
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
+  if (own_stream) cudaStreamDestroy(own_stream);
 }
-
-}  // namespace
-
-struct sq_handle {
-  sq::Deck deck;
-  sq::Setup setup;
-  sq_options opt{};
-  sq_info info{};
-  sq::LanczosParams lp{};
-  int num_sms = 0;
-  bool u_smem = false;
-  size_t smem = 0;
-  int grid = 0;
-  int block = 0;
-  int fermi_grid = 0;
-  size_t elem = 4;
-  // device buffers owned by the handle
-  sq::ImageMeta *d_images = nullptr;
-  void *d_tables = nullptr;
-  void *d_veff_ext = nullptr;
-  double *d_veff_in = nullptr;
-  void *d_u = nullptr;
-  void *d_proj = nullptr;
-  int *d_status = nullptr;
-  double *d_ab = nullptr;
-  long long ab_cap = 0;
-  long long last_n = 0;
-  double *d_lambda = nullptr, *d_w = nullptr, *d_lmin = nullptr, *d_lmax = nullptr;
-  long long out_cap = 0;
-  double *d_rho = nullptr;
-  long long rho_cap = 0;
-  double *d_fermi_scratch = nullptr;
-  unsigned *d_bar = nullptr;
-  double *d_fermi_out = nullptr;
-  int fermi_maxit = 400;
-  cudaStream_t own_stream = nullptr;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
-  bool ev_valid = false;
-
-  ~sq_handle() {
-    dev_free(d_images);
-    dev_free(d_tables);
-    dev_free(d_veff_ext);
-    dev_free(d_veff_in);
-    dev_free(d_u);
-    dev_free(d_proj);
-    dev_free(d_status);
-    dev_free(d_ab);
-    dev_free(d_lambda);
-    dev_free(d_w);
-    dev_free(d_lmin);
-    dev_free(d_lmax);
-    dev_free(d_rho);
-    dev_free(d_fermi_scratch);
-    dev_free(d_bar);
-    dev_free(d_fermi_out);
-    for (auto &e : ev)
-      if (e) cudaEventDestroy(e);
-    if (own_stream) cudaStreamDestroy(own_stream);
-  }
-};
 
 namespace {
 
@@ -187,13 +144,6 @@ long long max_box_points_per_node(const sq::Setup &s, const sq::Deck &d) {
   long long best = 0;
   for (long long v : acc) best = std::max(best, v);
   return best;
-}
-
-void ensure_capacity(double *&ptr, long long &cap, long long need, const char *what) {
-  if (need <= cap) return;
-  dev_free(ptr);
-  dev_alloc(&ptr, sizeof(double) * (size_t)need, what);
-  cap = need;
 }
 
 // Mean over all nodes of sum_images |box ∩ cube|.  The overlap of a box with the cube of
@@ -378,6 +328,10 @@ void build_engine(sq_handle *h) {
   fill_info(h->info, d, s, p.max_img, h->opt);
 }
 
+}  // namespace
+
+namespace sq {
+
 sq_status device_status(sq_handle *h, cudaStream_t s) {
   int st = 0;
   ck(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, s), "status D2H");
@@ -388,6 +342,19 @@ sq_status device_status(sq_handle *h, cudaStream_t s) {
     return fail(SQ_NO_CONVERGENCE, "Too many iterations in Tridiagonal solver");
   if (st & sq::kStatusBreakdown) return fail(SQ_LANCZOS_BREAKDOWN, "Lanczos breakdown (b_k == 0)");
   return SQ_OK;
+}
+
+void ensure_quadrature_buffers(sq_handle *h, long long n) {
+  const long long nq = n * h->lp.nqp;
+  long long cap = h->out_cap;
+  ensure_capacity(h->d_lambda, cap, nq, "lambda");
+  cap = h->out_cap;
+  ensure_capacity(h->d_w, cap, nq, "weights");
+  cap = h->out_cap;
+  ensure_capacity(h->d_lmin, cap, std::max(nq, n), "lambda_min");
+  cap = h->out_cap;
+  ensure_capacity(h->d_lmax, cap, std::max(nq, n), "lambda_max");
+  h->out_cap = std::max(h->out_cap, nq);
 }
 
 sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long long nb,
@@ -417,17 +384,8 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
   return SQ_OK;
 }
 
-template <typename F> sq_status guarded(F &&f) {
-  try {
-    return f();
-  } catch (const CudaError &e) {
-    return fail(SQ_CUDA_ERROR, e.what());
-  } catch (const std::exception &e) {
-    return fail(SQ_BAD_INPUT, e.what());
-  }
-}
 
-}  // namespace
+}  // namespace sq
 
 extern "C" {
 
@@ -510,15 +468,7 @@ sq_status sq_nodes_and_weights(sq_handle *h, const double *veff, double veff_con
     if (n <= 0 || node_begin < 0 || node_end > h->info.n_nodes)
       return fail(SQ_BAD_INPUT, "node range outside the grid");
     const long long q = h->lp.nqp;
-    long long cap = h->out_cap;
-    ensure_capacity(h->d_lambda, cap, n * q, "lambda");
-    cap = h->out_cap;
-    ensure_capacity(h->d_w, cap, n * q, "weights");
-    cap = h->out_cap;
-    ensure_capacity(h->d_lmin, cap, std::max(n * q, n), "lambda_min");
-    cap = h->out_cap;
-    ensure_capacity(h->d_lmax, cap, std::max(n * q, n), "lambda_max");
-    h->out_cap = std::max(h->out_cap, n * q);
+    ensure_quadrature_buffers(h, n);
     const double *dv = nullptr;
     if (veff) {
       ck(cudaMemcpyAsync(h->d_veff_in, veff, sizeof(double) * h->info.n_nodes,
@@ -591,15 +541,7 @@ sq_status sq_fermi_density_energy(sq_handle *h, const double *lambda, const doub
     ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
     cudaStream_t s = h->own_stream;
     const long long nq = (long long)n_nodes * h->lp.nqp;
-    long long cap = h->out_cap;
-    ensure_capacity(h->d_lambda, cap, nq, "lambda");
-    cap = h->out_cap;
-    ensure_capacity(h->d_w, cap, nq, "weights");
-    cap = h->out_cap;
-    ensure_capacity(h->d_lmin, cap, nq, "lambda_min");
-    cap = h->out_cap;
-    ensure_capacity(h->d_lmax, cap, nq, "lambda_max");
-    h->out_cap = std::max(h->out_cap, nq);
+    ensure_quadrature_buffers(h, n_nodes);
     ensure_capacity(h->d_rho, h->rho_cap, n_nodes, "rho");
     ck(cudaMemcpyAsync(h->d_lambda, lambda, sizeof(double) * nq, cudaMemcpyHostToDevice, s), "H2D");
     ck(cudaMemcpyAsync(h->d_w, weights, sizeof(double) * nq, cudaMemcpyHostToDevice, s), "H2D");
@@ -655,6 +597,6 @@ sq_status sq_measure_fp32_peak(int device, double *tflops) {
   });
 }
 
-const char *sq_last_error_string(void) { return g_last_error.c_str(); }
+const char *sq_last_error_string(void) { return sq::last_error().c_str(); }
 
 }  // extern "C"

@@ -56,6 +56,7 @@ void parse_inpt(Deck &d, const std::string &path) {
       {"PULAY_FREQUENCY:", [&] { d.pulay_frequency = ts.next_int("PULAY_FREQUENCY"); }},
       {"TOL_SCF:", [&] { d.tol_scf = ts.next_double("TOL_SCF"); }},
       {"MAXIT_SCF:", [&] { d.maxit_scf = ts.next_int("MAXIT_SCF"); }},
+      {"REFERENCE_CUTOFF:", [&] { d.reference_cutoff = ts.next_double("REFERENCE_CUTOFF"); }},
       {"NTYPE:", [&] {
          ntype = ts.next_int("NTYPE");
          if (ntype <= 0 || ntype > kMaxTypes) throw std::runtime_error("NTYPE must be 1..8");

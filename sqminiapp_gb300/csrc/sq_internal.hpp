@@ -97,6 +97,7 @@ struct Deck {
   int pulay_frequency = 1;
   double tol_scf = 1e-6;
   int maxit_scf = 100;
+  double reference_cutoff = 0.5;  // src/lsdft_readfiles.cc:80
   std::string xc = "LDA";
   std::vector<int> lloc;
   std::vector<std::string> psd_file;
