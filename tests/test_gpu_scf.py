@@ -100,3 +100,23 @@ def test_warm_start_from_device_density(cell, oracle_result):
                 break
     assert r["converged"] == 1 and its <= 4
     assert r["free_energy_per_atom"] == pytest.approx(oracle_result["free_energy_per_atom"], abs=1e-6)
+
+
+def test_density_checkpoint_restart_and_output_echo(cell, oracle_result, tmp_path):
+    """An SCF restarted from a .den checkpoint (Read_ElecDens, the reference's READ_DEN_FILE
+    warm start) converges at once; the .out echo lists the deck's parameters."""
+    from sqminiapp_gb300 import LSDFT, Print_ElecDens, Read_ElecDens
+    d, name, o, fields = cell
+    shape = fields["b"].shape
+    with LSDFT(d, name, faithful=False, precision=64) as eng:
+        r1 = eng.SCF_LSSGQ(tol=1e-7, maxit=120)
+        rho, _ = eng.scf_density()
+        Print_ElecDens(str(tmp_path / "ck"), rho.reshape(shape))
+        back = Read_ElecDens(str(tmp_path / "ck"), shape)
+        r2 = eng.SCF_LSSGQ(rho_init=back, tol=1e-6, maxit=10)
+        eng.write_output_echo(str(tmp_path / "run.out"))
+    assert r2["iterations"] <= 4
+    assert r2["free_energy_per_atom"] == pytest.approx(r1["free_energy_per_atom"], abs=1e-7)
+    text = open(tmp_path / "run.out").read()
+    nx, ny, nz = o.grid
+    assert "FD_GRID: %d %d %d" % (nx, ny, nz) in text and "EXCHANGE_CORRELATION: LDA_PW" in text
