@@ -233,6 +233,43 @@ sq_status sq_scf_history(sq_handle *h, int cap, double *free_energy, double *res
 /* Host evaluation of the LDA functional the SCF uses: eps_xc and Vxc per density value. */
 sq_status sq_lda_pw92(const double *rho, long n, double *eps, double *v);
 
+/* ---- Learned warm start (no counterpart in the reference, whose SCF starts from the atomic
+ * superposition, SuperposAtRho, src/ilsdft.h:269).  A 64-128-128-1 MLP with SiLU activations
+ * maps 64 rotation-invariant neighbour descriptors of each grid point (16 Gaussian radial
+ * centres over 0-8 bohr times l = 0..3) to the correction rho_SCF - rho_0; BF16 weights and
+ * activations, FP32 accumulation on the tensor cores (tcgen05), Adam training on the GPU. */
+typedef struct sq_mlp sq_mlp;
+#define SQ_MLP_N_PARAMS 24961  /* W1[64][128], b1[128], W2[128][128], b2[128], w3[128], b3 */
+/* A network with He-initialised weights on `device`. */
+sq_status sq_mlp_create(int device, unsigned long long seed, sq_mlp **out);
+void sq_mlp_destroy(sq_mlp *m);
+sq_status sq_mlp_save(const sq_mlp *m, const char *path);
+sq_status sq_mlp_load(const char *path, int device, sq_mlp **out);
+/* FP32 master parameters (SQ_MLP_N_PARAMS, layout above), feature standardisation
+ * (mean[64], 1/std[64]; NULL keeps the current one) and target scale. */
+sq_status sq_mlp_set_params(sq_mlp *m, const float *params, const float *feat_mean,
+                            const float *feat_inv_std, double t_mean, double t_std);
+sq_status sq_mlp_get_params(const sq_mlp *m, float *params, float *feat_mean,
+                            float *feat_inv_std, double *t_mean, double *t_std);
+/* Raw descriptors of every node of the handle's cell, HOST [n_nodes][64]. */
+sq_status sq_descriptors(sq_handle *h, float *desc);
+/* Add the handle's cell as training samples: descriptors and rho_out - rho_0 of its last SCF. */
+sq_status sq_mlp_add_training_cell(sq_mlp *m, sq_handle *h);
+/* Adam steps (tiles_per_step tiles of 128 samples each step, learning rate lr); the first
+ * call fixes the standardisation from the samples.  final_loss: mean squared error of the
+ * last step in standardised units. */
+sq_status sq_mlp_train(sq_mlp *m, int steps, int tiles_per_step, double lr, double *final_loss);
+/* Loss and gradients (SQ_MLP_N_PARAMS) of mean((y - t)^2) over n standardised samples
+ * x [n][64], t [n] (HOST), computed by the tensor-core training kernel. */
+sq_status sq_mlp_gradients(sq_mlp *m, const float *x, const float *t, long n, double *loss,
+                           float *grads);
+/* Network outputs y [n] (standardised units) of standardised features x [n][64] (HOST). */
+sq_status sq_mlp_forward(sq_mlp *m, const float *x, long n, float *y);
+/* Predicted density rho_0 + correction of the handle's cell, HOST [n_nodes]. */
+sq_status sq_mlp_predict_density(sq_mlp *m, sq_handle *h, double *rho);
+/* sq_scf_begin from the network's predicted density (cut at zero, scaled to N_e). */
+sq_status sq_scf_begin_learned(sq_handle *h, const sq_scf_options *opt, sq_mlp *m);
+
 /* ---- The reference's text files (one block of the grid per rank; one GPU: corner 0, dims =
  * FD_GRID).  Files are "<prefix>_<rank>.den" / ".lambdas"; reading fails with SQ_BAD_INPUT
  * when the header's block differs from corner/dims. */

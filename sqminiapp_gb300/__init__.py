@@ -23,15 +23,20 @@ import numpy as np
 from .capi import SQ_OK, SqError, SqInfo, SqOptions, SqScfOptions, SqScfResult, lib, check, library_path
 
 __all__ = ["LSDFT", "SqError", "library_path", "DECK_DIR", "lda_pw92", "Print_ElecDens",
-           "Read_ElecDens", "Print_MinMaxLambda", "Read_MinMaxLambda"]
+           "Read_ElecDens", "Print_MinMaxLambda", "Read_MinMaxLambda", "WarmStartMLP"]
 
 DECK_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "decks")
 
 _dp = ctypes.POINTER(ctypes.c_double)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 
 def _ptr(a):
     return a.ctypes.data_as(_dp)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(_fp)
 
 
 class LSDFT:
@@ -199,7 +204,7 @@ class LSDFT:
 
     def SCF_LSSGQ(self, rho_init=None, tol=None, maxit=None, mixing_parameter=None,
                   mixing_history=None, pulay_frequency=None, fermi_tol=None, kerker_ktf=None,
-                  raise_on_maxit=True):
+                  raise_on_maxit=True, model=None):
         """Self-consistent field loop on the GPU until ||rho_out - rho_in|| / ||rho_out|| < tol.
 
         rho_init: None (superposition of atomic valence densities) or a host density over the
@@ -209,6 +214,20 @@ class LSDFT:
         last iteration with the per-iteration history of free energy and residual."""
         opt = self._scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency,
                                 fermi_tol, kerker_ktf)
+        if model is not None:
+            # learned start (sq_scf_begin_learned), then the same loop one step at a time
+            check(self._lib.sq_scf_begin_learned(self._h, ctypes.byref(opt), model._m),
+                  "sq_scf_begin_learned")
+            limit = self._deck_maxit() if not maxit else int(maxit)
+            out = {}
+            for _ in range(limit):
+                out = self.scf_step()
+                if out["converged"]:
+                    break
+            if not out.get("converged") and raise_on_maxit:
+                raise SqError(2, "SCF_LSSGQ", "SCF did not reach TOL_SCF within MAXIT_SCF iterations")
+            out["free_energy_history"], out["residual_history"] = self.scf_history()
+            return out
         rp = None
         if rho_init is not None:
             rho_init = np.ascontiguousarray(rho_init, dtype=np.float64).reshape(-1)
@@ -222,6 +241,17 @@ class LSDFT:
         out = res.as_dict()
         out["free_energy_history"], out["residual_history"] = self.scf_history()
         return out
+
+    def _deck_maxit(self):
+        # MAXIT_SCF of the deck is not in sq_info; a learned start runs at most 100 steps by
+        # default, the reference's MAXIT_SCF default
+        return 100
+
+    def descriptors(self):
+        """The 64 neighbour descriptors of every node [n_nodes, 64] (FP32)."""
+        d = np.empty((self.n_nodes, 64), dtype=np.float32)
+        check(self._lib.sq_descriptors(self._h, _fptr(d)), "sq_descriptors")
+        return d
 
     def scf_begin(self, rho_init=None, d_rho_init=None, **opts):
         """Start an SCF by hand (then call scf_step); d_rho_init is a device address."""
@@ -326,3 +356,100 @@ def Read_MinMaxLambda(prefix, shape, rank=0, corner=(0, 0, 0)):
     check(lib().sq_read_lambda_file(str(prefix).encode(), int(rank), c, d, _ptr(lo), _ptr(hi)),
           "sq_read_lambda_file")
     return lo, hi
+
+
+class WarmStartMLP:
+    """The learned SCF start: a 64-128-128-1 BF16 MLP trained on the GPU (tensor-core kernels)
+    to predict rho_SCF - rho_0 from the 64 neighbour descriptors of each node."""
+
+    N_PARAMS = 24961
+    SHAPES = (("W1", (64, 128)), ("b1", (128,)), ("W2", (128, 128)), ("b2", (128,)),
+              ("w3", (128,)), ("b3", (1,)))
+
+    def __init__(self, device=0, seed=1, path=None):
+        self._lib = lib()
+        self._m = ctypes.c_void_p()
+        if path is not None:
+            check(self._lib.sq_mlp_load(str(path).encode(), int(device), ctypes.byref(self._m)),
+                  "sq_mlp_load")
+        else:
+            check(self._lib.sq_mlp_create(int(device), int(seed), ctypes.byref(self._m)),
+                  "sq_mlp_create")
+
+    def close(self):
+        if self._m:
+            self._lib.sq_mlp_destroy(self._m)
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def save(self, path):
+        check(self._lib.sq_mlp_save(self._m, str(path).encode()), "sq_mlp_save")
+
+    @classmethod
+    def _split(cls, flat):
+        out, o = {}, 0
+        for name, shape in cls.SHAPES:
+            n = int(np.prod(shape))
+            out[name] = flat[o:o + n].reshape(shape).copy()
+            o += n
+        return out
+
+    @classmethod
+    def _join(cls, params):
+        return np.concatenate([np.asarray(params[n], dtype=np.float32).reshape(-1)
+                               for n, _ in cls.SHAPES])
+
+    def get_params(self):
+        flat = np.empty(self.N_PARAMS, dtype=np.float32)
+        mean = np.empty(64, dtype=np.float32)
+        istd = np.empty(64, dtype=np.float32)
+        tm, ts = ctypes.c_double(), ctypes.c_double()
+        check(self._lib.sq_mlp_get_params(self._m, _fptr(flat), _fptr(mean), _fptr(istd),
+                                          ctypes.byref(tm), ctypes.byref(ts)), "sq_mlp_get_params")
+        p = self._split(flat)
+        p.update(feat_mean=mean, feat_inv_std=istd, t_mean=tm.value, t_std=ts.value)
+        return p
+
+    def set_params(self, params, feat_mean=None, feat_inv_std=None, t_mean=0.0, t_std=1.0):
+        flat = np.ascontiguousarray(self._join(params), dtype=np.float32)
+        fm = None if feat_mean is None else _fptr(np.ascontiguousarray(feat_mean, np.float32))
+        fi = None if feat_inv_std is None else _fptr(np.ascontiguousarray(feat_inv_std, np.float32))
+        check(self._lib.sq_mlp_set_params(self._m, _fptr(flat), fm, fi, float(t_mean), float(t_std)),
+              "sq_mlp_set_params")
+
+    def gradients(self, x, t):
+        """(loss, grads dict) of mean((y - t)^2) from the tensor-core training kernel."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        g = np.empty(self.N_PARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        check(self._lib.sq_mlp_gradients(self._m, _fptr(x), _fptr(t), len(t), ctypes.byref(loss),
+                                         _fptr(g)), "sq_mlp_gradients")
+        return loss.value, self._split(g)
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.empty(len(x), dtype=np.float32)
+        check(self._lib.sq_mlp_forward(self._m, _fptr(x), len(x), _fptr(y)), "sq_mlp_forward")
+        return y
+
+    def add_training_cell(self, engine):
+        """Samples from an engine whose SCF has run: descriptors and rho_out - rho_0."""
+        check(self._lib.sq_mlp_add_training_cell(self._m, engine._h), "sq_mlp_add_training_cell")
+
+    def train(self, steps, tiles_per_step=152, lr=1e-3):
+        loss = ctypes.c_double()
+        check(self._lib.sq_mlp_train(self._m, int(steps), int(tiles_per_step), float(lr),
+                                     ctypes.byref(loss)), "sq_mlp_train")
+        return loss.value
+
+    def predict_density(self, engine):
+        rho = np.empty(engine.n_nodes)
+        check(self._lib.sq_mlp_predict_density(self._m, engine._h, _ptr(rho)),
+              "sq_mlp_predict_density")
+        return rho

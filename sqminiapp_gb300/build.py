@@ -30,6 +30,7 @@ SOURCES = {
     "scf_setup.cpp": [],
     "scf.cu": [],
     "io.cpp": [],
+    "mlp.cu": ["-Xptxas", "-v"],
 }
 
 

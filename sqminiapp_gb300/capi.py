@@ -15,6 +15,7 @@ _vp = ctypes.c_void_p
 _l = ctypes.c_long
 _d = ctypes.c_double
 _ip = ctypes.POINTER(ctypes.c_int)
+_fp = ctypes.POINTER(ctypes.c_float)
 
 
 class SqOptions(ctypes.Structure):
@@ -83,6 +84,19 @@ SIGNATURES = {
     "sq_write_lambda_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, _dp, _dp]),
     "sq_read_lambda_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _ip, _ip, _dp, _dp]),
     "sq_write_output_echo": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "sq_mlp_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_vp)]),
+    "sq_mlp_destroy": (None, [_vp]),
+    "sq_mlp_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
+    "sq_mlp_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_vp)]),
+    "sq_mlp_set_params": (ctypes.c_int, [_vp, _fp, _fp, _fp, _d, _d]),
+    "sq_mlp_get_params": (ctypes.c_int, [_vp, _fp, _fp, _fp, _dp, _dp]),
+    "sq_descriptors": (ctypes.c_int, [_vp, _fp]),
+    "sq_mlp_add_training_cell": (ctypes.c_int, [_vp, _vp]),
+    "sq_mlp_train": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _d, _dp]),
+    "sq_mlp_gradients": (ctypes.c_int, [_vp, _fp, _fp, _l, _dp, _fp]),
+    "sq_mlp_forward": (ctypes.c_int, [_vp, _fp, _l, _fp]),
+    "sq_mlp_predict_density": (ctypes.c_int, [_vp, _vp, _dp]),
+    "sq_scf_begin_learned": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _vp]),
     "sq_last_error_string": (ctypes.c_char_p, []),
 }
 

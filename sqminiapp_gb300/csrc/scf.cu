@@ -561,6 +561,12 @@ sq_status step(sq_handle *h, sq_scf_result *res, cudaStream_t st) {
 
 }  // namespace
 
+double *scf_rho0_device(sq_handle *h) { return scf_state(h).d_rho0; }
+double *scf_rho_out_device(sq_handle *h) { return scf_state(h).d_rho_out; }
+void scf_begin_device_density(sq_handle *h, const sq_scf_options *o, const double *d_rho) {
+  begin(h, o, d_rho, true, h->own_stream);
+}
+
 }  // namespace sq
 
 using namespace sq;

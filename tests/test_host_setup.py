@@ -83,3 +83,13 @@ def test_python_wrapper_fails_loudly_without_library(monkeypatch):
     monkeypatch.setattr(capi, "_LIB", "/nonexistent/libsq_gb300.so")
     with pytest.raises(ImportError):
         capi.lib()
+
+
+def test_mlp_parameter_count_matches_layout():
+    """SQ_MLP_N_PARAMS (the host buffers' size) is the 64-128-128-1 layout's count."""
+    import re
+    from sqminiapp_gb300 import WarmStartMLP
+    n = sum(int(np.prod(s)) for _, s in WarmStartMLP.SHAPES)
+    assert n == WarmStartMLP.N_PARAMS == 64 * 128 + 128 + 128 * 128 + 128 + 128 + 1
+    hdr = open(os.path.join(ROOT, "include", "sq_gb300.h")).read()
+    assert int(re.search(r"#define SQ_MLP_N_PARAMS (\d+)", hdr).group(1)) == n
