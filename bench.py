@@ -41,6 +41,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD = "mg32_h0.5_rc6.5_q40"
 SCF_WORKLOAD = "mg4_h0.5_rc6_q30"
+WARM_START_MODEL = os.path.join(ROOT, "sqminiapp_gb300", "models", "warm_start_h0.5_rc6.5_q40.bin")
+WARM_START_DISCRETISATION = {"h": 0.5, "rcut": 6.5, "n_qp": 40}
 METRIC = "node-Lanczos/s"
 
 
@@ -61,6 +63,9 @@ def parse_args():
                    help="cell of the time-to-SCF leg ('none' skips it)")
     p.add_argument("--scf-precisions", default="32,64",
                    help="engines timed by the time-to-SCF leg")
+    p.add_argument("--scf-model", default=WARM_START_MODEL,
+                   help="learned start for the FP32 engine ('none' skips it); used when the cell "
+                        "has the discretisation the model was trained at")
     return p.parse_args()
 
 
@@ -334,6 +339,7 @@ def scf_leg(args, local):
     sq_scf_run from the atomic-superposition start; engine setup timed apart)."""
     from sqminiapp_gb300 import LSDFT
     (deck_dir, name, meta), cfg = make_deck(args.scf_config, 0)
+    cfg.setdefault("n_qp", cfg.get("n_qp"))
     out = {"workload": args.scf_config, "atoms": meta["natoms"], "start": "atomic superposition",
            "stop": "relative density residual < TOL_SCF (1e-6; 3e-5 floor for FP32 vectors)"}
     for prec in [int(p) for p in args.scf_precisions.split(",") if p]:
@@ -350,6 +356,27 @@ def scf_leg(args, local):
                               "residual": r["residual"], "tol": r["tol"],
                               "sq_seconds": r["sq_ms"] / 1e3}
         eng.close()
+    model_ok = (args.scf_model != "none" and os.path.exists(args.scf_model) and
+                all(cfg[k] == v for k, v in WARM_START_DISCRETISATION.items()))
+    if model_ok and 32 in [int(p) for p in args.scf_precisions.split(",") if p]:
+        from sqminiapp_gb300 import WarmStartMLP
+        model = WarmStartMLP(device=local, path=args.scf_model)
+        eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local)
+        eng.scf_begin()
+        t0 = time.perf_counter()
+        r = eng.SCF_LSSGQ(raise_on_maxit=False, model=model)  # descriptors + MLP inside
+        wall = time.perf_counter() - t0
+        out["fp32_learned"] = {"seconds": wall, "iterations": r["iterations"],
+                               "converged": bool(r["converged"]),
+                               "free_energy_per_atom": r["free_energy_per_atom"],
+                               "residual": r["residual"], "tol": r["tol"],
+                               "model": os.path.basename(args.scf_model)}
+        eng.close()
+        model.close()
+        if "fp64" in out:
+            out["speedup_fp32_learned_vs_fp64"] = out["fp64"]["seconds"] / wall
+            out["dF_per_atom_fp32_learned_vs_fp64"] = abs(r["free_energy_per_atom"] -
+                                                          out["fp64"]["free_energy_per_atom"])
     if "fp32" in out and "fp64" in out:
         out["speedup_fp32_vs_fp64"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
         out["dF_per_atom_fp32_vs_fp64"] = abs(out["fp32"]["free_energy_per_atom"] -
