@@ -145,6 +145,22 @@ sq_status sq_fermi_density_energy_device(sq_handle *h, const double *d_lambda,
 sq_status sq_electron_count_device(sq_handle *h, const double *d_lambda, const double *d_weights,
                                    long n_nodes, double lambda_f, double *count, void *stream);
 
+/* Mixed-cell batch: every node of n_cells independent cells (each its own handle, with its
+ * own mesh, Rcut, N_qp and precision) in one submission.  The reference runs one cell per job
+ * (NodesAndWeights_LSSGQ, src/lsdft.h:132).  The GPU's SMs are split between the cells so that
+ * they finish together: by each cell's measured cost per node and SM once every handle has run
+ * before, else by its algorithmic FLOPs per node (at least one SM each).  Each cell's
+ * persistent Lanczos kernel runs on its handle's stream on its share of SMs, concurrently with
+ * the others, and `stream` waits for all of them.  Per cell c: d_veff[c] (DEVICE, NULL =
+ * constant veff_const[c]; d_veff and veff_const may be NULL), outputs d_lambda[c],
+ * d_weights[c] [n_nodes][n_qp], d_lambda_min[c], d_lambda_max[c] [n_nodes].  Synchronises the
+ * cells' streams to report their status. */
+sq_status sq_batch_nodes_and_weights(sq_handle *const *cells, int n_cells,
+                                     const double *const *d_veff, const double *veff_const,
+                                     double *const *d_lambda, double *const *d_weights,
+                                     double *const *d_lambda_min, double *const *d_lambda_max,
+                                     void *stream);
+
 /* Device time (ms) of the kernels of the last nodes_and_weights call, measured with CUDA
  * events on the stream they ran on: ms[0] Lanczos kernel, ms[1] quadrature kernel. */
 sq_status sq_last_kernel_times(sq_handle *h, double *ms);

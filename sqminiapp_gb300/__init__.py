@@ -23,7 +23,8 @@ import numpy as np
 from .capi import SQ_OK, SqError, SqInfo, SqOptions, SqScfOptions, SqScfResult, lib, check, library_path
 
 __all__ = ["LSDFT", "SqError", "library_path", "DECK_DIR", "lda_pw92", "Print_ElecDens",
-           "Read_ElecDens", "Print_MinMaxLambda", "Read_MinMaxLambda", "WarmStartMLP"]
+           "Read_ElecDens", "Print_MinMaxLambda", "Read_MinMaxLambda", "WarmStartMLP",
+           "batch_nodes_and_weights"]
 
 DECK_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "decks")
 
@@ -453,3 +454,21 @@ class WarmStartMLP:
         check(self._lib.sq_mlp_predict_density(self._m, engine._h, _ptr(rho)),
               "sq_mlp_predict_density")
         return rho
+
+
+def batch_nodes_and_weights(engines, veffs=None, veff_consts=None, outputs=None, stream=0):
+    """All nodes of several cells (one LSDFT each) in one batched submission
+    (sq_batch_nodes_and_weights): the SMs are split so that the cells finish together and the
+    cells' kernels run concurrently.  veffs: per cell a device address of its FD-grid Veff
+    (FP64) or None; outputs: per cell a dict of device addresses lambda, weights, lambda_min,
+    lambda_max.  Asynchronous on `stream` apart from the final status check."""
+    n = len(engines)
+    vp = ctypes.c_void_p
+    hs = (vp * n)(*[e._h for e in engines])
+    dv = None if veffs is None else (vp * n)(*[v or None for v in veffs])
+    vc = None if veff_consts is None else (ctypes.c_double * n)(*[float(c) for c in veff_consts])
+    cols = {k: (vp * n)(*[o[k] for o in outputs]) for k in ("lambda", "weights", "lambda_min",
+                                                              "lambda_max")}
+    check(lib().sq_batch_nodes_and_weights(hs, n, dv, vc, cols["lambda"], cols["weights"],
+                                           cols["lambda_min"], cols["lambda_max"], vp(stream)),
+          "sq_batch_nodes_and_weights")

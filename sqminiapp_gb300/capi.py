@@ -97,6 +97,10 @@ SIGNATURES = {
     "sq_mlp_forward": (ctypes.c_int, [_vp, _fp, _l, _fp]),
     "sq_mlp_predict_density": (ctypes.c_int, [_vp, _vp, _dp]),
     "sq_scf_begin_learned": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _vp]),
+    "sq_batch_nodes_and_weights": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int,
+                                                  ctypes.POINTER(_vp), _dp, ctypes.POINTER(_vp),
+                                                  ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                                  ctypes.POINTER(_vp), _vp]),
     "sq_last_error_string": (ctypes.c_char_p, []),
 }
 

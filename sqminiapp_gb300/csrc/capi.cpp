@@ -10,6 +10,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "handle.hpp"
 #include "sq_gb300.h"
@@ -357,9 +358,22 @@ void ensure_quadrature_buffers(sq_handle *h, long long n) {
   h->out_cap = std::max(h->out_cap, nq);
 }
 
+void update_node_cost(sq_handle *h) {
+  if (!h->ev_valid || h->cost_nodes <= 0) return;
+  if (cudaEventQuery(h->ev[1]) != cudaSuccess) {
+    cudaGetLastError();  // a pending event is not an error
+    return;
+  }
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]) == cudaSuccess && ms > 0.f)
+    h->node_sm_ms = (double)ms * h->cost_grid / (double)h->cost_nodes;
+  cudaGetLastError();
+  h->cost_nodes = 0;
+}
+
 sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long long nb,
                      long long ne, double *d_lambda, double *d_w, double *d_lmin, double *d_lmax,
-                     cudaStream_t s) {
+                     cudaStream_t s, int grid_limit) {
   const long long n = ne - nb;
   if (nb < 0 || ne > h->info.n_nodes || n <= 0)
     return fail(SQ_BAD_INPUT, "node range outside the grid");
@@ -369,17 +383,25 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
   p.node_end = ne;
   ck(cudaMemsetAsync(h->d_status, 0, sizeof(int), s), "status reset");
   ck(sq::launch_veff_extend(d_veff, veff_const, h->d_veff_ext, h->opt.precision, p, s), "veff");
-  const int grid = (int)std::min<long long>(h->grid, n);
-  ck(cudaEventRecord(h->ev[0], s), "event");
+  const int grid = (int)std::min<long long>(grid_limit > 0 ? std::min(grid_limit, h->grid) : h->grid, n);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ck(cudaStreamIsCapturing(s, &cap), "capture status");
+  const bool timed = cap == cudaStreamCaptureStatusNone;  // no timing events inside a graph
+  if (timed) {
+    update_node_cost(h);
+    h->cost_grid = grid;
+    h->cost_nodes = n;
+    ck(cudaEventRecord(h->ev[0], s), "event");
+  }
   ck(sq::launch_lanczos(p, h->opt.precision, h->opt.faithful != 0, h->u_smem, grid, h->block, h->smem, s,
                         h->d_veff_ext, h->d_images, h->d_tables, h->d_u, h->d_proj, h->d_ab,
                         h->d_status),
      "lanczos");
-  ck(cudaEventRecord(h->ev[1], s), "event");
+  if (timed) ck(cudaEventRecord(h->ev[1], s), "event");
   ck(sq::launch_quadrature(h->d_ab, n, p.nqp, d_lambda, d_w, d_lmin, d_lmax, h->d_status, s),
      "quadrature");
-  ck(cudaEventRecord(h->ev[2], s), "event");
-  h->ev_valid = true;
+  if (timed) ck(cudaEventRecord(h->ev[2], s), "event");
+  h->ev_valid = timed;
   h->last_n = n;
   return SQ_OK;
 }
@@ -593,6 +615,82 @@ sq_status sq_measure_fp32_peak(int device, double *tflops) {
   return guarded([&] {
     ck(cudaSetDevice(device), "cudaSetDevice");
     ck(sq::measure_fp32_peak(device, tflops), "fp32 probe");
+    return SQ_OK;
+  });
+}
+
+sq_status sq_batch_nodes_and_weights(sq_handle *const *cells, int n_cells, const double *const *d_veff,
+                                     const double *veff_const, double *const *d_lambda,
+                                     double *const *d_weights, double *const *d_lambda_min,
+                                     double *const *d_lambda_max, void *stream) {
+  if (!cells || n_cells <= 0 || !d_lambda || !d_weights || !d_lambda_min || !d_lambda_max)
+    return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    for (int c = 0; c < n_cells; c++) {
+      if (!cells[c] || !d_lambda[c] || !d_weights[c] || !d_lambda_min[c] || !d_lambda_max[c])
+        return fail(SQ_BAD_INPUT, "null cell argument");
+      if (cells[c]->opt.device != cells[0]->opt.device)
+        return fail(SQ_BAD_INPUT, "all cells of a batch on one device");
+      for (int o = 0; o < c; o++)
+        if (cells[o] == cells[c]) return fail(SQ_BAD_INPUT, "a handle appears twice in the batch");
+    }
+    ck(cudaSetDevice(cells[0]->opt.device), "cudaSetDevice");
+    const int sms = cells[0]->num_sms;
+    if (n_cells > sms) return fail(SQ_BAD_INPUT, "more cells than SMs in one batch");
+    // Work per cell: nodes x the measured cost of a node on one SM when every cell has run
+    // before (the split then follows the kernels' real speeds), else nodes x per-node FLOPs.
+    bool measured = true;
+    for (int c = 0; c < n_cells; c++) {
+      update_node_cost(cells[c]);
+      if (!(cells[c]->node_sm_ms > 0.0)) measured = false;
+    }
+    std::vector<double> per_node(n_cells);
+    for (int c = 0; c < n_cells; c++) {
+      const sq_info &in = cells[c]->info;
+      const double nc = (double)in.cube[0] * in.cube[1] * in.cube[2];
+      per_node[c] = measured ? cells[c]->node_sm_ms
+                             : in.n_qp * ((2.0 * (6 * in.fd_half_order + 1) + 9.0) * nc +
+                                          4.0 * in.n_lm * in.proj_points_per_node);
+    }
+    // one SM each, then every further SM to the cell that would finish last; a cell's finish
+    // time counts whole rounds of nodes, ceil(nodes / SMs) x cost per node
+    std::vector<int> share(n_cells, 1);
+    auto finish = [&](int c, int sh) {
+      return std::ceil((double)cells[c]->info.n_nodes / sh) * per_node[c];
+    };
+    for (int left = sms - n_cells; left > 0; left--) {
+      int worst = 0;
+      for (int c = 1; c < n_cells; c++)
+        if (finish(c, share[c]) > finish(worst, share[worst])) worst = c;
+      if (share[worst] >= cells[worst]->info.n_nodes) break;  // more SMs would idle
+      share[worst]++;
+    }
+    // fork: every cell's stream waits for the caller's stream and runs its cell on its SM
+    // share; the caller's stream waits for all of them
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t fork = nullptr;
+    ck(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
+    std::vector<cudaEvent_t> join(n_cells, nullptr);
+    sq_status st = SQ_OK;
+    ck(cudaEventRecord(fork, s), "event");
+    for (int c = 0; c < n_cells && st == SQ_OK; c++) {
+      sq_handle *h = cells[c];
+      ck(cudaStreamWaitEvent(h->own_stream, fork, 0), "wait");
+      st = run_device(h, d_veff ? d_veff[c] : nullptr, veff_const ? veff_const[c] : 0.0, 0,
+                      h->info.n_nodes, d_lambda[c], d_weights[c], d_lambda_min[c],
+                      d_lambda_max[c], h->own_stream, share[c]);
+      ck(cudaEventCreateWithFlags(&join[c], cudaEventDisableTiming), "event");
+      ck(cudaEventRecord(join[c], h->own_stream), "event");
+      ck(cudaStreamWaitEvent(s, join[c], 0), "wait");
+    }
+    cudaEventDestroy(fork);
+    for (cudaEvent_t e : join)
+      if (e) cudaEventDestroy(e);
+    if (st != SQ_OK) return st;
+    for (int c = 0; c < n_cells; c++) {
+      st = device_status(cells[c], cells[c]->own_stream);
+      if (st != SQ_OK) return st;
+    }
     return SQ_OK;
   });
 }

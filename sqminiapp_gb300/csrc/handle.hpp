@@ -87,6 +87,11 @@ struct sq_handle {
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   bool ev_valid = false;
   sq::ScfState *scf = nullptr;  // SCF closure state, created by the first SCF call
+  // measured cost of one node on one SM (ms), from the events of the last Lanczos launch;
+  // mixed-cell batches split the SMs by it
+  double node_sm_ms = 0.0;
+  int cost_grid = 0;
+  long long cost_nodes = 0;
 
   ~sq_handle();
 };
@@ -94,9 +99,13 @@ struct sq_handle {
 namespace sq {
 
 // Per-node Lanczos + quadrature of nodes [nb, ne) on stream s (device buffers).
+// grid_limit > 0 caps the persistent grid (CTAs = SMs used), else one CTA per SM.
 sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long long nb,
                      long long ne, double *d_lambda, double *d_w, double *d_lmin, double *d_lmax,
-                     cudaStream_t s);
+                     cudaStream_t s, int grid_limit = 0);
+// Folds the timing of the last Lanczos launch, once its events have completed, into
+// node_sm_ms (non-blocking).
+void update_node_cost(sq_handle *h);
 // Synchronises s and turns the device status bits into a status code.
 sq_status device_status(sq_handle *h, cudaStream_t s);
 // Grows the handle's lambda / weight / lambda_min / lambda_max arrays to n nodes.
