@@ -203,6 +203,9 @@ typedef struct sq_scf_options {
   double kerker_ktf;        /* Kerker preconditioner k_TF (1/bohr) of the mixing: > 0 that value,
                                0 the default 1.0 (the reference mixes preconditioned,
                                src/lsdft_readfiles.cc:102), < 0 no preconditioner */
+  int cuda_graph;           /* 1: from the second iteration on, replay one captured CUDA graph
+                               of the iteration's device part (Poisson, potential, Lanczos,
+                               quadrature); 0: direct launches */
 } sq_scf_options;
 
 typedef struct sq_scf_result {

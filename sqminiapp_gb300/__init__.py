@@ -198,14 +198,15 @@ class LSDFT:
     # --- SCF closure (SCF_LSSGQ, src/lsdft.h:153) -----------------------------------------
     @staticmethod
     def _scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency, fermi_tol,
-                     kerker_ktf=None):
+                     kerker_ktf=None, cuda_graph=False):
         return SqScfOptions(float(tol or 0.0), int(maxit or 0), float(mixing_parameter or 0.0),
                             int(mixing_history or 0), int(pulay_frequency or 0),
-                            float(fermi_tol or 0.0), float(kerker_ktf or 0.0))
+                            float(fermi_tol or 0.0), float(kerker_ktf or 0.0),
+                            int(bool(cuda_graph)))
 
     def SCF_LSSGQ(self, rho_init=None, tol=None, maxit=None, mixing_parameter=None,
                   mixing_history=None, pulay_frequency=None, fermi_tol=None, kerker_ktf=None,
-                  raise_on_maxit=True, model=None):
+                  raise_on_maxit=True, model=None, cuda_graph=False):
         """Self-consistent field loop on the GPU until ||rho_out - rho_in|| / ||rho_out|| < tol.
 
         rho_init: None (superposition of atomic valence densities) or a host density over the
@@ -214,7 +215,7 @@ class LSDFT:
         k_TF = 1/bohr, negative = unpreconditioned mixing.  Returns the result dict of the
         last iteration with the per-iteration history of free energy and residual."""
         opt = self._scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency,
-                                fermi_tol, kerker_ktf)
+                                fermi_tol, kerker_ktf, cuda_graph)
         if model is not None:
             # learned start (sq_scf_begin_learned), then the same loop one step at a time
             check(self._lib.sq_scf_begin_learned(self._h, ctypes.byref(opt), model._m),
@@ -258,7 +259,8 @@ class LSDFT:
         """Start an SCF by hand (then call scf_step); d_rho_init is a device address."""
         opt = self._scf_options(opts.get("tol"), opts.get("maxit"), opts.get("mixing_parameter"),
                                 opts.get("mixing_history"), opts.get("pulay_frequency"),
-                                opts.get("fermi_tol"), opts.get("kerker_ktf"))
+                                opts.get("fermi_tol"), opts.get("kerker_ktf"),
+                                opts.get("cuda_graph"))
         if d_rho_init is not None:
             check(self._lib.sq_scf_begin_device(self._h, ctypes.byref(opt),
                                                 ctypes.c_void_p(d_rho_init)), "sq_scf_begin_device")

@@ -285,8 +285,13 @@ struct ScfState {
   bool converged = false;
   std::vector<double> hist_F, hist_err;
   sq_scf_result last{};
+  // CUDA graph of an iteration's device part (Poisson, potential, SQ pass)
+  bool use_graph = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  const double *graph_lambda = nullptr;  // the quadrature buffer the graph writes
 
   ~ScfState() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (plans) {
       cufftDestroy(plan_f);
       cufftDestroy(plan_i);
@@ -415,6 +420,12 @@ void begin(sq_handle *h, const sq_scf_options *o, const double *rho_init, bool r
   if (s.history > kMaxHistory)
     throw std::invalid_argument("MIXING_HISTORY above " + std::to_string(kMaxHistory) + " is not supported");
   if (s.pulay_every < 1) s.pulay_every = 1;
+  s.use_graph = o && o->cuda_graph != 0;
+  if (s.graph_exec) {  // captured anew at the second iteration of this run
+    cudaGraphExecDestroy(s.graph_exec);
+    s.graph_exec = nullptr;
+  }
+  s.graph_lambda = nullptr;
   s.iter = 0;
   s.have_prev = 0;
   s.hist_count = 0;
@@ -448,16 +459,49 @@ sq_status step(sq_handle *h, sq_scf_result *res, cudaStream_t st) {
   const Deck &d = h->deck;
   const double dV = h->setup.dV;
   const auto t0 = std::chrono::steady_clock::now();
-  // potential of rho_in
-  poisson(s, s.d_rho_in, s.d_phi, st);
-  potential_kernel<<<kRedBlocks, kBlock, 0, st>>>(s.d_rho_in, s.d_phi, s.d_b, s.d_vxc, s.d_veff,
-                                                  s.ng, s.d_part);
-  ck(cudaGetLastError(), "potential");
-  finish_sums<<<1, 256, 0, st>>>(s.d_part, kRedBlocks, 3, s.d_sums + kMaxSums - 3);
-  ck(cudaGetLastError(), "finish sums");
-  // SQ pass and Fermi level
+  // potential of rho_in, then the SQ pass: direct launches, or (cuda_graph) the first
+  // iteration direct and every later one a replay of one captured graph of the same launches
+  // (its buffers are fixed from sq_scf_begin on)
   ensure_quadrature_buffers(h, s.ng);
-  sq_status rs = run_device(h, s.d_veff, 0.0, 0, s.ng, h->d_lambda, h->d_w, h->d_lmin, h->d_lmax, st);
+  auto device_part = [&](cudaStream_t q) -> sq_status {
+    poisson(s, s.d_rho_in, s.d_phi, q);
+    potential_kernel<<<kRedBlocks, kBlock, 0, q>>>(s.d_rho_in, s.d_phi, s.d_b, s.d_vxc, s.d_veff,
+                                                   s.ng, s.d_part);
+    ck(cudaGetLastError(), "potential");
+    finish_sums<<<1, 256, 0, q>>>(s.d_part, kRedBlocks, 3, s.d_sums + kMaxSums - 3);
+    ck(cudaGetLastError(), "finish sums");
+    return run_device(h, s.d_veff, 0.0, 0, s.ng, h->d_lambda, h->d_w, h->d_lmin, h->d_lmax, q);
+  };
+  sq_status rs = SQ_OK;
+  if (s.use_graph && s.graph_lambda != h->d_lambda && s.iter > 0) {
+    if (s.graph_exec) {
+      cudaGraphExecDestroy(s.graph_exec);
+      s.graph_exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    ck(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    rs = device_part(st);  // recorded, not run
+    const cudaError_t ec = cudaStreamEndCapture(st, &g);
+    if (rs != SQ_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rs;
+    }
+    ck(ec, "end capture");
+    ck(cudaGraphInstantiate(&s.graph_exec, g, 0), "graph instantiate");
+    cudaGraphDestroy(g);
+    s.graph_lambda = h->d_lambda;
+  }
+  if (s.use_graph && s.graph_exec && s.graph_lambda == h->d_lambda) {
+    // the handle's timing events bracket the whole graph (potential + SQ pass)
+    ck(cudaEventRecord(h->ev[0], st), "event");
+    ck(cudaGraphLaunch(s.graph_exec, st), "graph launch");
+    ck(cudaEventRecord(h->ev[1], st), "event");
+    ck(cudaEventRecord(h->ev[2], st), "event");
+    h->ev_valid = true;
+    h->last_n = s.ng;
+  } else {
+    rs = device_part(st);
+  }
   if (rs != SQ_OK) return rs;
   // the Lanczos status bits stay set: device_status below reports them with the Fermi ones
   ck(launch_fermi(h->d_lambda, h->d_w, s.ng, h->lp.nqp, h->info.beta, d.n_electrons, dV,
