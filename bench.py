@@ -25,6 +25,7 @@ Multi-GPU (torchrun): one rank per GPU, each rank an independent cell (seed + ra
 collective on the data path (weak scaling); max time over ranks.
 """
 import argparse
+import math
 import json
 import os
 import statistics
@@ -180,7 +181,9 @@ def run_reference(args):
         "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded FCC Mg cell)",
         "config": {"workload": args.config, "n_nodes": meta["N"] ** 3, "atoms": meta["natoms"],
-                   "cube": cfg["rcut"], "n_qp": cfg["n_qp"]},
+                   "grid": [meta["N"]] * 3, "cube": [2 * math.ceil(cfg["rcut"] / meta["h"]) + 1] * 3,
+                   "n_qp": cfg["n_qp"], "rcut": cfg["rcut"], "h": meta["h"], "operator": "corrected",
+                   "precision": "fp64 (CPU restatement of the reference path)"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": samples[-1] + "; FP64 restatement of the reference path "
                          "(PETSc/MPI reference not buildable here)"},
