@@ -35,6 +35,16 @@ template <typename P> void dev_free(P *&ptr) {
   ptr = nullptr;
 }
 
+// Device buffer owned by a scope: freed on every exit path, exceptions included.
+template <typename P> struct DevBuf {
+  P *p = nullptr;
+  DevBuf(size_t bytes, const char *what) { dev_alloc(&p, bytes, what); }
+  ~DevBuf() { dev_free(p); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  P *get() const { return p; }
+};
+
 // Grows a device array of doubles to at least `need` elements (contents are not kept).
 void ensure_capacity(double *&ptr, long long &cap, long long need, const char *what);
 

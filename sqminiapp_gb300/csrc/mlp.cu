@@ -712,8 +712,8 @@ std::vector<float4> neighbour_images(const Deck &d) {
 void compute_descriptors(sq_handle *h, float *d_out, cudaStream_t s) {
   const Deck &d = h->deck;
   std::vector<float4> img = neighbour_images(d);
-  float4 *d_img = nullptr;
-  dev_alloc(&d_img, sizeof(float4) * std::max<size_t>(1, img.size()), "images");
+  DevBuf<float4> buf(sizeof(float4) * std::max<size_t>(1, img.size()), "images");
+  float4 *d_img = buf.get();
   ck(cudaMemcpyAsync(d_img, img.data(), sizeof(float4) * img.size(), cudaMemcpyHostToDevice, s), "images H2D");
   const long long n = h->info.n_nodes;
   descriptor_kernel<<<grid_of(n * 32, 256), 256, 0, s>>>(
@@ -721,7 +721,6 @@ void compute_descriptors(sq_handle *h, float *d_out, cudaStream_t s) {
       (float)h->setup.h[2], (float)d.cell_half[0], (float)d.cell_half[1], (float)d.cell_half[2], n, d_out);
   ck_launch("descriptors");
   ck(cudaStreamSynchronize(s), "sync");
-  dev_free(d_img);
 }
 
 // standardisation from the stored raw samples (means and standard deviations per feature)
@@ -773,8 +772,15 @@ void pack_training_set(sq_mlp *m, cudaStream_t s) {
   m->packed_samples = n;
 }
 
-// One forward+backward over the given tiles (host list); gradients into d_grad.
-void run_train_kernel(sq_mlp *m, const std::vector<int> &tiles, int per_cta, float inv_count, cudaStream_t s) {
+// Packed samples a training kernel reads: feature tiles in both layouts, targets, row masks.
+struct TileSet {
+  const uint8_t *xa, *xt;
+  const float *t, *mask;
+};
+
+// One forward+backward over the given tiles (host list) of `set`; gradients into d_grad.
+void run_train_kernel(sq_mlp *m, const TileSet &set, const std::vector<int> &tiles, int per_cta,
+                      float inv_count, cudaStream_t s) {
   const int G = (int)(tiles.size() / per_cta);
   if ((int)tiles.size() > m->tiles_cap) {
     dev_free(m->d_tiles);
@@ -787,7 +793,7 @@ void run_train_kernel(sq_mlp *m, const std::vector<int> &tiles, int per_cta, flo
     m->partial_rows = G;
   }
   ck(cudaMemcpyAsync(m->d_tiles, tiles.data(), sizeof(int) * tiles.size(), cudaMemcpyHostToDevice, s), "tiles H2D");
-  mlp_train_kernel<<<G, 128, kTrSmem, s>>>(m->d_xa, m->d_xt, m->d_t, m->d_mask, m->d_tiles, per_cta, m->d_w1p,
+  mlp_train_kernel<<<G, 128, kTrSmem, s>>>(set.xa, set.xt, set.t, set.mask, m->d_tiles, per_cta, m->d_w1p,
                                            m->d_w2p, m->d_w2tp, m->d_params, inv_count, m->d_partial,
                                            m->d_status);
   ck_launch("mlp train");
@@ -798,10 +804,10 @@ void run_train_kernel(sq_mlp *m, const std::vector<int> &tiles, int per_cta, flo
 // network output for every node of the handle's cell -> d_y (n_nodes floats)
 void predict_y(sq_mlp *m, sq_handle *h, float *d_y, cudaStream_t s) {
   const long long n = h->info.n_nodes, nt = (n + kTile - 1) / kTile, np = nt * kTile;
-  float *d_raw = nullptr;
-  uint8_t *d_xa = nullptr;
-  dev_alloc(&d_raw, sizeof(float) * (size_t)n * kFeat, "descriptors");
-  dev_alloc(&d_xa, (size_t)nt * kXTileBytes, "tiles");
+  DevBuf<float> raw(sizeof(float) * (size_t)n * kFeat, "descriptors");
+  DevBuf<uint8_t> xa(sizeof(uint8_t) * (size_t)nt * kXTileBytes, "tiles");
+  float *d_raw = raw.get();
+  uint8_t *d_xa = xa.get();
   compute_descriptors(h, d_raw, s);
   pack_features_kernel<<<grid_of(np * kFeat), 256, 0, s>>>(d_raw, n, np, m->d_mean, m->d_istd, d_xa, nullptr);
   ck_launch("pack features");
@@ -810,8 +816,6 @@ void predict_y(sq_mlp *m, sq_handle *h, float *d_y, cudaStream_t s) {
   mlp_forward_kernel<<<grid, 128, kFwdSmem, s>>>(d_xa, nt, n, m->d_w1p, m->d_w2p, m->d_params, d_y, m->d_status);
   ck_launch("mlp forward");
   ck(cudaStreamSynchronize(s), "sync");
-  dev_free(d_raw);
-  dev_free(d_xa);
 }
 
 }  // namespace
@@ -934,11 +938,9 @@ sq_status sq_descriptors(sq_handle *h, float *desc) {
   return guarded([&] {
     ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
     const long long n = h->info.n_nodes;
-    float *d = nullptr;
-    dev_alloc(&d, sizeof(float) * (size_t)n * kFeat, "descriptors");
-    compute_descriptors(h, d, h->own_stream);
-    ck(cudaMemcpy(desc, d, sizeof(float) * (size_t)n * kFeat, cudaMemcpyDeviceToHost), "descriptors D2H");
-    dev_free(d);
+    DevBuf<float> d(sizeof(float) * (size_t)n * kFeat, "descriptors");
+    compute_descriptors(h, d.get(), h->own_stream);
+    ck(cudaMemcpy(desc, d.get(), sizeof(float) * (size_t)n * kFeat, cudaMemcpyDeviceToHost), "descriptors D2H");
     return SQ_OK;
   });
 }
@@ -994,7 +996,7 @@ sq_status sq_mlp_train(sq_mlp *m, int steps, int tiles_per_step, double lr, doub
     for (int it = 0; it < steps; it++) {
       for (int &t : tiles) t = (int)pick(m->rng);
       pack_weights(m, s);
-      run_train_kernel(m, tiles, per_cta, inv_count, s);
+      run_train_kernel(m, TileSet{m->d_xa, m->d_xt, m->d_t, m->d_mask}, tiles, per_cta, inv_count, s);
       m->adam_step++;
       const double c1 = 1.0 / (1.0 - std::pow(0.9, (double)m->adam_step));
       const double c2 = 1.0 / (1.0 - std::pow(0.999, (double)m->adam_step));
@@ -1022,46 +1024,27 @@ sq_status sq_mlp_gradients(sq_mlp *m, const float *x, const float *t, long n, do
     ck(cudaSetDevice(m->device), "cudaSetDevice");
     cudaStream_t s = 0;
     const long long nt = (n + kTile - 1) / kTile, np = nt * kTile;
-    float *d_x = nullptr, *d_t = nullptr, *d_tp = nullptr, *d_mask = nullptr, *d_zero = nullptr, *d_one = nullptr;
-    uint8_t *d_xa = nullptr, *d_xt = nullptr;
-    dev_alloc(&d_x, sizeof(float) * (size_t)n * kFeat, "x");
-    dev_alloc(&d_t, sizeof(float) * n, "t");
-    dev_alloc(&d_tp, sizeof(float) * np, "t");
-    dev_alloc(&d_mask, sizeof(float) * np, "mask");
-    dev_alloc(&d_xa, (size_t)nt * kXTileBytes, "xa");
-    dev_alloc(&d_xt, (size_t)nt * kXTileBytes, "xt");
-    dev_alloc(&d_zero, sizeof(float) * kFeat, "zero");
-    dev_alloc(&d_one, sizeof(float) * kFeat, "one");
+    DevBuf<float> x_d(sizeof(float) * (size_t)n * kFeat, "x"), t_d(sizeof(float) * n, "t"),
+        tp_d(sizeof(float) * np, "t"), mask_d(sizeof(float) * np, "mask"),
+        zero_d(sizeof(float) * kFeat, "zero"), one_d(sizeof(float) * kFeat, "one");
+    DevBuf<uint8_t> xa_d((size_t)nt * kXTileBytes, "xa"), xt_d((size_t)nt * kXTileBytes, "xt");
     std::vector<float> z(kFeat, 0.f), o(kFeat, 1.f);
-    ck(cudaMemcpy(d_zero, z.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
-    ck(cudaMemcpy(d_one, o.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
-    ck(cudaMemcpy(d_x, x, sizeof(float) * (size_t)n * kFeat, cudaMemcpyHostToDevice), "x H2D");
-    ck(cudaMemcpy(d_t, t, sizeof(float) * n, cudaMemcpyHostToDevice), "t H2D");
-    pack_features_kernel<<<grid_of(np * kFeat), 256, 0, s>>>(d_x, n, np, d_zero, d_one, d_xa, d_xt);
-    pack_targets_kernel<<<grid_of(np), 256, 0, s>>>(d_t, n, np, 0.f, 1.f, d_tp, d_mask);
+    ck(cudaMemcpy(zero_d.get(), z.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemcpy(one_d.get(), o.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemcpy(x_d.get(), x, sizeof(float) * (size_t)n * kFeat, cudaMemcpyHostToDevice), "x H2D");
+    ck(cudaMemcpy(t_d.get(), t, sizeof(float) * n, cudaMemcpyHostToDevice), "t H2D");
+    pack_features_kernel<<<grid_of(np * kFeat), 256, 0, s>>>(x_d.get(), n, np, zero_d.get(), one_d.get(),
+                                                             xa_d.get(), xt_d.get());
+    pack_targets_kernel<<<grid_of(np), 256, 0, s>>>(t_d.get(), n, np, 0.f, 1.f, tp_d.get(), mask_d.get());
     ck_launch("pack");
-    std::swap(m->d_xa, d_xa);
-    std::swap(m->d_xt, d_xt);
-    std::swap(m->d_t, d_tp);
-    std::swap(m->d_mask, d_mask);
-    const long long saved_tiles = m->ntiles, saved_packed = m->packed_samples;
-    m->ntiles = nt;
     // every tile once, one tile per CTA
     std::vector<int> tiles((size_t)nt);
     for (long long i = 0; i < nt; i++) tiles[i] = (int)i;
     pack_weights(m, s);
-    run_train_kernel(m, tiles, 1, 1.0f / (float)n, s);
+    run_train_kernel(m, TileSet{xa_d.get(), xt_d.get(), tp_d.get(), mask_d.get()}, tiles, 1,
+                     1.0f / (float)n, s);
     std::vector<float> g(kPartial);
     ck(cudaMemcpy(g.data(), m->d_grad, sizeof(float) * kPartial, cudaMemcpyDeviceToHost), "grad D2H");
-    std::swap(m->d_xa, d_xa);
-    std::swap(m->d_xt, d_xt);
-    std::swap(m->d_t, d_tp);
-    std::swap(m->d_mask, d_mask);
-    m->ntiles = saved_tiles;
-    m->packed_samples = saved_packed;
-    for (float *p : {d_x, d_t, d_tp, d_mask, d_zero, d_one}) dev_free(p);
-    dev_free(d_xa);
-    dev_free(d_xt);
     sq_status st = mlp_status(m);
     if (st != SQ_OK) return st;
     std::memcpy(grads, g.data(), sizeof(float) * kParams);
@@ -1076,26 +1059,22 @@ sq_status sq_mlp_forward(sq_mlp *m, const float *x, long n, float *y) {
     ck(cudaSetDevice(m->device), "cudaSetDevice");
     cudaStream_t s = 0;
     const long long nt = (n + kTile - 1) / kTile, np = nt * kTile;
-    float *d_x = nullptr, *d_y = nullptr, *d_zero = nullptr, *d_one = nullptr;
-    uint8_t *d_xa = nullptr;
-    dev_alloc(&d_x, sizeof(float) * (size_t)n * kFeat, "x");
-    dev_alloc(&d_y, sizeof(float) * n, "y");
-    dev_alloc(&d_xa, (size_t)nt * kXTileBytes, "xa");
-    dev_alloc(&d_zero, sizeof(float) * kFeat, "zero");
-    dev_alloc(&d_one, sizeof(float) * kFeat, "one");
+    DevBuf<float> x_d(sizeof(float) * (size_t)n * kFeat, "x"), y_d(sizeof(float) * n, "y"),
+        zero_d(sizeof(float) * kFeat, "zero"), one_d(sizeof(float) * kFeat, "one");
+    DevBuf<uint8_t> xa_d((size_t)nt * kXTileBytes, "xa");
     std::vector<float> z(kFeat, 0.f), o(kFeat, 1.f);
-    ck(cudaMemcpy(d_zero, z.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
-    ck(cudaMemcpy(d_one, o.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
-    ck(cudaMemcpy(d_x, x, sizeof(float) * (size_t)n * kFeat, cudaMemcpyHostToDevice), "x H2D");
-    pack_features_kernel<<<grid_of(np * kFeat), 256, 0, s>>>(d_x, n, np, d_zero, d_one, d_xa, nullptr);
+    ck(cudaMemcpy(zero_d.get(), z.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemcpy(one_d.get(), o.data(), sizeof(float) * kFeat, cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemcpy(x_d.get(), x, sizeof(float) * (size_t)n * kFeat, cudaMemcpyHostToDevice), "x H2D");
+    pack_features_kernel<<<grid_of(np * kFeat), 256, 0, s>>>(x_d.get(), n, np, zero_d.get(), one_d.get(),
+                                                             xa_d.get(), nullptr);
     ck_launch("pack");
     pack_weights(m, s);
     const int grid = (int)std::min<long long>(nt, 2LL * m->num_sms);
-    mlp_forward_kernel<<<grid, 128, kFwdSmem, s>>>(d_xa, nt, n, m->d_w1p, m->d_w2p, m->d_params, d_y, m->d_status);
+    mlp_forward_kernel<<<grid, 128, kFwdSmem, s>>>(xa_d.get(), nt, n, m->d_w1p, m->d_w2p, m->d_params,
+                                                   y_d.get(), m->d_status);
     ck_launch("mlp forward");
-    ck(cudaMemcpy(y, d_y, sizeof(float) * n, cudaMemcpyDeviceToHost), "y D2H");
-    for (float *p : {d_x, d_y, d_zero, d_one}) dev_free(p);
-    dev_free(d_xa);
+    ck(cudaMemcpy(y, y_d.get(), sizeof(float) * n, cudaMemcpyDeviceToHost), "y D2H");
     return mlp_status(m);
   });
 }
@@ -1105,17 +1084,14 @@ sq_status sq_mlp_predict_density(sq_mlp *m, sq_handle *h, double *rho) {
   return guarded([&] {
     ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
     const long long n = h->info.n_nodes;
-    float *d_y = nullptr;
-    double *d_rho = nullptr;
-    dev_alloc(&d_y, sizeof(float) * n, "y");
-    dev_alloc(&d_rho, sizeof(double) * n, "rho");
-    predict_y(m, h, d_y, h->own_stream);
-    correction_kernel<<<grid_of(n), 256, 0, h->own_stream>>>(scf_rho0_device(h), d_y, m->t_mean, m->t_std, n, d_rho);
+    DevBuf<float> y_d(sizeof(float) * n, "y");
+    DevBuf<double> rho_d(sizeof(double) * n, "rho");
+    predict_y(m, h, y_d.get(), h->own_stream);
+    correction_kernel<<<grid_of(n), 256, 0, h->own_stream>>>(scf_rho0_device(h), y_d.get(), m->t_mean,
+                                                             m->t_std, n, rho_d.get());
     ck_launch("correction");
-    ck(cudaMemcpyAsync(rho, d_rho, sizeof(double) * n, cudaMemcpyDeviceToHost, h->own_stream), "rho D2H");
+    ck(cudaMemcpyAsync(rho, rho_d.get(), sizeof(double) * n, cudaMemcpyDeviceToHost, h->own_stream), "rho D2H");
     ck(cudaStreamSynchronize(h->own_stream), "sync");
-    dev_free(d_y);
-    dev_free(d_rho);
     return mlp_status(m);
   });
 }
@@ -1125,17 +1101,14 @@ sq_status sq_scf_begin_learned(sq_handle *h, const sq_scf_options *opt, sq_mlp *
   return guarded([&] {
     ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
     const long long n = h->info.n_nodes;
-    float *d_y = nullptr;
-    double *d_rho = nullptr;
-    dev_alloc(&d_y, sizeof(float) * n, "y");
-    dev_alloc(&d_rho, sizeof(double) * n, "rho");
-    predict_y(m, h, d_y, h->own_stream);
-    correction_kernel<<<grid_of(n), 256, 0, h->own_stream>>>(scf_rho0_device(h), d_y, m->t_mean, m->t_std, n, d_rho);
+    DevBuf<float> y_d(sizeof(float) * n, "y");
+    DevBuf<double> rho_d(sizeof(double) * n, "rho");
+    predict_y(m, h, y_d.get(), h->own_stream);
+    correction_kernel<<<grid_of(n), 256, 0, h->own_stream>>>(scf_rho0_device(h), y_d.get(), m->t_mean,
+                                                             m->t_std, n, rho_d.get());
     ck_launch("correction");
     sq_status st = mlp_status(m);
-    if (st == SQ_OK) scf_begin_device_density(h, opt, d_rho);
-    dev_free(d_y);
-    dev_free(d_rho);
+    if (st == SQ_OK) scf_begin_device_density(h, opt, rho_d.get());  // copies rho; synchronises
     return st;
   });
 }
