@@ -228,6 +228,12 @@ typedef struct sq_scf_result {
                               with FP32 Lanczos vectors (their residual noise floor is ~1e-5) */
 } sq_scf_result;
 
+/* Host-only report of a periodic deck's fixed SCF fields (no GPU touched): pseudocharges
+ * b[n_nodes], atomic-superposition density rho0[n_nodes], the Poisson symbol green on the
+ * R2C half grid [Nz][Ny][Nx/2+1], and scalars[4] = E_self, E_self of the reference
+ * pseudocharges, E_c, int b.  Any output may be NULL. */
+sq_status sq_describe_scf_fields(const char *deck_dir, const char *name, double *b, double *rho0,
+                                 double *green, double *scalars);
 /* Start an SCF: rho_init HOST [n_nodes] (NULL = superposition of the psd atomic valence
  * densities, SuperposAtRho of src/ilsdft.h:269), cut at zero and scaled to the electron
  * count.  opt may be NULL (deck values).  Clears the mixing history. */

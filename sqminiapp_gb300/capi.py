@@ -101,6 +101,8 @@ SIGNATURES = {
                                                   ctypes.POINTER(_vp), _dp, ctypes.POINTER(_vp),
                                                   ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                                   ctypes.POINTER(_vp), _vp]),
+    "sq_describe_scf_fields": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _dp, _dp, _dp,
+                                              _dp]),
     "sq_last_error_string": (ctypes.c_char_p, []),
 }
 

@@ -14,6 +14,7 @@
 
 #include "handle.hpp"
 #include "sq_gb300.h"
+#include "scf_internal.hpp"
 #include "sq_internal.hpp"
 #include "sq_kernels.hpp"
 
@@ -449,6 +450,26 @@ sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful,
         for (int l = 0; l < 4; l++) gamma[4 * t + l] = s.types[t].gamma[l];
       if (cutoff)
         for (int a = 0; a < 3; a++) cutoff[3 * t + a] = s.pseudocharge_cutoff[3 * t + a];
+    }
+    return SQ_OK;
+  });
+}
+
+sq_status sq_describe_scf_fields(const char *deck_dir, const char *name, double *b, double *rho0,
+                                 double *green, double *scalars) {
+  if (!deck_dir || !name) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] {
+    sq::Deck d = sq::read_deck(deck_dir, name);
+    sq::Setup s = sq::build_setup(d, false);
+    sq::ScfFields f = sq::build_scf_fields(d, s);
+    if (b) std::copy(f.b.begin(), f.b.end(), b);
+    if (rho0) std::copy(f.rho0.begin(), f.rho0.end(), rho0);
+    if (green) std::copy(f.green.begin(), f.green.end(), green);
+    if (scalars) {
+      scalars[0] = f.e_self;
+      scalars[1] = f.e_self_ref;
+      scalars[2] = f.e_corr;
+      scalars[3] = f.b_total;
     }
     return SQ_OK;
   });

@@ -135,3 +135,27 @@ def test_oracle_scf_converges(small_scf):
     r2 = scf(o, fields, tol=1e-6, maxit=6, rho_init=r["rho_out"])
     assert r2["iterations"] <= 4 and r2["converged"]
     assert r2["free_energy_per_atom"] == pytest.approx(r["free_energy_per_atom"], abs=1e-6)
+
+
+def test_library_scf_fields_match_oracle(small_scf, small_cell):
+    """The product's host construction of the fixed SCF fields (scf_setup.cpp, reported
+    without a GPU) against the oracle's independent numpy construction."""
+    import ctypes
+    from sqminiapp_gb300.capi import check, lib
+    o, ref = small_scf
+    d, name, _ = small_cell
+    nx, ny, nz = o.grid
+    dp = ctypes.POINTER(ctypes.c_double)
+    b = np.zeros(nx * ny * nz)
+    rho0 = np.zeros(nx * ny * nz)
+    green = np.zeros(nz * ny * (nx // 2 + 1))
+    sc = np.zeros(4)
+    check(lib().sq_describe_scf_fields(d.encode(), name.encode(), b.ctypes.data_as(dp),
+                                       rho0.ctypes.data_as(dp), green.ctypes.data_as(dp),
+                                       sc.ctypes.data_as(dp)), "sq_describe_scf_fields")
+    shape = ref["b"].shape
+    assert np.max(np.abs(b.reshape(shape) - ref["b"])) <= 1e-12 * np.max(np.abs(ref["b"]))
+    assert np.max(np.abs(rho0.reshape(shape) - ref["rho0"])) <= 1e-12 * np.max(ref["rho0"])
+    np.testing.assert_allclose(green.reshape(ref["green"].shape), ref["green"], rtol=1e-12, atol=0)
+    for k, v in zip(("e_self", "e_self_ref", "e_corr", "b_total"), sc):
+        assert v == pytest.approx(ref[k], rel=1e-10, abs=1e-12), k
