@@ -140,3 +140,24 @@ def test_cuda_graph_scf_matches_direct_launches(cell):
         assert r["free_energy"] == pytest.approx(a["free_energy"], rel=1e-9)
         np.testing.assert_allclose(r["free_energy_history"][:5], a["free_energy_history"][:5],
                                    rtol=1e-9)
+
+
+def test_bench_cell_scf_matches_oracle_golden(tmp_path):
+    """Full-size SCF of the 4-atom bench cell (17^3 nodes, 25^3 cubes, 30 Lanczos steps)
+    against the CPU oracle's run committed in tests/golden/scf_mg4.json (made by
+    tests/golden/make_scf_golden.py): FP64 to 1e-8 Ha/atom, FP32 within the 1e-5 target."""
+    import json
+    import os
+    from sqminiapp_gb300 import LSDFT
+    from sqminiapp_gb300.decks import CONFIGS, make_fcc_mg_deck
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "scf_mg4.json")))
+    d, name, _ = make_fcc_mg_deck(str(tmp_path), "cell", seed=g["seed"], **CONFIGS[g["config"]])
+    with LSDFT(d, name, faithful=False, precision=64) as eng:
+        r64 = eng.SCF_LSSGQ(tol=g["tol"], maxit=60)
+    with LSDFT(d, name, faithful=False, precision=32) as eng:
+        r32 = eng.SCF_LSSGQ(maxit=60)
+    assert r64["iterations"] == g["iterations"]
+    assert r64["free_energy_per_atom"] == pytest.approx(g["free_energy_per_atom"], abs=1e-8)
+    assert r64["lambda_f"] == pytest.approx(g["lambda_f"], abs=1e-7)
+    assert r32["converged"] == 1
+    assert r32["free_energy_per_atom"] == pytest.approx(g["free_energy_per_atom"], abs=1e-5)
