@@ -20,6 +20,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", CSR
 SOURCES = {
     "lanczos.cu": [],
     "lanczos_f32.cu": ["-Xptxas", "-v"],
+    "lanczos_f32w.cu": ["-Xptxas", "-v"],
     "lanczos_f64.cu": ["-Xptxas", "-v"],
     "quadrature.cu": ["-fmad=false"],
     "fermi.cu": [],

@@ -268,7 +268,9 @@ void build_engine(sq_handle *h) {
   for (int r = rank; r < sq::kMaxLm; r++) p.rank_l[r] = 0;
   p.alpha_stride = h->opt.faithful ? 1 : rank;
 
-  if (p.nx > 32) throw std::invalid_argument("cubes wider than 32 points in x are not supported");
+  const bool wide = p.nx > 32;
+  if (wide && h->opt.precision != 32)
+    throw std::invalid_argument("cubes wider than 32 points in x need FP32 vectors");
   if (d.n_qp > 64) throw std::invalid_argument("LANCZOS_DEGREE above 64 is not supported");
 
   const int need_img = std::max(1, max_images_per_node(s, d));
@@ -277,9 +279,13 @@ void build_engine(sq_handle *h) {
   const int maxw = h->opt.precision == 32 ? sq::kMaxWarpsF32 : sq::kMaxWarpsF64;
   p.rows_per_warp = (p.ny + maxw - 1) / maxw;
   h->block = 32 * ((p.ny + p.rows_per_warp - 1) / p.rows_per_warp);
+  if (wide) {  // one thread per (row, x pair)
+    const int tasks = p.ny * ((p.nx + 1) / 2);
+    h->block = 32 * std::min(sq::kWideWarpsF32, (tasks + 31) / 32);
+  }
   const bool faithful = h->opt.faithful != 0;
   h->u_smem = false;
-  if (h->opt.precision == 32 &&
+  if (h->opt.precision == 32 && !wide &&
       sq::lanczos_smem_bytes(p, 4, true, faithful) <= (size_t)smem_optin)
     h->u_smem = true;
   h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
@@ -289,7 +295,7 @@ void build_engine(sq_handle *h) {
                                 " does not fit in shared memory at this precision");
   h->grid = h->num_sms;
   {  // projector records pack the P and U indices of a cube point into 16 bits each
-    const long long pitch_rows = (h->opt.precision == 32) ? p.ny + 2 * sq::kStencilHalf : p.ny;
+    const long long pitch_rows = (h->opt.precision == 32) ? p.ny + sq::kStencilHalf : p.ny;
     const long long psize = (long long)sq::kStencilHalf * p.pitch + (long long)p.nz * pitch_rows * p.pitch;
     if (psize >= 65536 || (long long)p.upitch * p.ny * p.nz >= 65536)
       throw std::invalid_argument("truncated cube too large for 16-bit point indices");

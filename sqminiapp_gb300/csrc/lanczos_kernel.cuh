@@ -9,13 +9,17 @@
 // Layout.  A persistent CTA (one per SM) owns one node at a time and keeps both Lanczos
 // vectors on chip:
 //   P  the stencil source, with 6 zero columns between rows (x) and, in FP32, 6 zero rows
-//      above and below every z-plane (y), so no neighbour load needs a bounds check;
+//      between consecutive z-planes and before the first (y): row -d of a plane is a zero
+//      row of the gap before it, row ny-1+d one of the gap after it, so no neighbour load
+//      needs a bounds check;
 //   U  the elementwise vector (v_{k-1}, then the new residual); in shared memory when both
 //      fit, else in a per-CTA slice of global scratch.
 // Vector passes (FP32): a half-warp owns one y-row and a z-range; each lane computes the x
 // pair (x, x+1) from 64-bit shared loads, forming neighbour sums with Blackwell's packed
 // add.rn.f32x2, and walks z with a 13-plane register ring, so one output costs ~10 shared
-// loads.  FP64 uses one warp per row with scalar loads.
+// loads.  Cubes wider than 32 points (WIDE) give each thread one (row, x pair) over all of
+// z instead, consecutive threads on consecutive pairs.  FP64 uses one warp per row with
+// scalar loads.
 // Nonlocal term: when a node starts, its projector matrix restricted to the cube (support
 // points only) is written once to a per-CTA list in global scratch: per point the packed
 // P/U indices and chi_lm (chi_lm = T_l(r) P_lm(x,y,z), from the per-atom radial tables and
@@ -248,8 +252,8 @@ __device__ __forceinline__ void decode(const ImgView<T> &v, int t, int &lx, int 
   ly = row - lz * v.ey;
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD>
-__global__ void __launch_bounds__(512, 1)
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD, bool WIDE>
+__global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
     lanczos_kernel(const __grid_constant__ LanczosParams p, const T *__restrict__ veff_ext,
                    const ImageMeta *__restrict__ images, const T *__restrict__ tables,
                    T *__restrict__ u_global, unsigned char *proj_scratch,
@@ -262,9 +266,9 @@ __global__ void __launch_bounds__(512, 1)
   const int nw = blockDim.x >> 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
-  // P index of (x,y,z) = OFF + z*PS + y*pitch + x.  YPAD: every z-plane carries O zero rows
-  // above and below, so y-neighbours need no bounds checks either.
-  const int PS = (YPAD ? ny + 2 * O : ny) * pitch;
+  // P index of (x,y,z) = OFF + z*PS + y*pitch + x.  YPAD: O zero rows precede every z-plane
+  // and follow the last, so y-neighbours need no bounds checks either.
+  const int PS = (YPAD ? ny + O : ny) * pitch;
   const int OFF = YPAD ? O * pitch : O;
   const int upitch = p.upitch;  // U row pitch (nx, or nx+1 to keep FP32 pairs aligned)
   const int US = ny * upitch;   // U plane stride
@@ -328,9 +332,11 @@ __global__ void __launch_bounds__(512, 1)
   const int zlen = (nz + nzs - 1) / nzs;
   const int zb = zc * zlen, ze = min(nz, zb + zlen);
   const int px = 2 * hl;
-  const bool pact = PAIRED && py < ny && px < nx && zb < ze;
+  const bool pact = PAIRED && !WIDE && py < ny && px < nx && zb < ze;
   const int phi = (px + 1 < nx) ? 1 : 0;
   const int pxc = px < nx ? px : ((nx - 1) & ~1);
+  // WIDE: task t = (row t / npairs, pair t % npairs), all of z
+  const int npairs = (nx + 1) >> 1, ntask = ny * npairs;
 
   for (long long node = p.node_begin + blockIdx.x; node < p.node_end; node += gridDim.x) {
     const int I = (int)(node % p.Nx);
@@ -567,24 +573,26 @@ __global__ void __launch_bounds__(512, 1)
         float2 *U2 = reinterpret_cast<float2 *>(U);
         const int PS2 = PS >> 1, pitch2 = pitch >> 1, US2 = US >> 1;
         const int VS = p.EY * p.EX;
-        if (pact) {
-          const int rowP2 = (OFF + py * pitch + pxc) >> 1;
-          const int rowU2 = (py * upitch + pxc) >> 1;
-          const float *vrow = veff_ext + ((size_t)K * p.EY + (J + py)) * p.EX + (I + pxc);
+        // one (row ry, pair rx..rx+1, z-range [rzb, rze)) item; rphi = pair has a second point
+        auto pair_pass1 = [&](const int ry, const int rx, const int rphi, const int rzb,
+                              const int rze) {
+          const int rowP2 = (OFF + ry * pitch + rx) >> 1;
+          const int rowU2 = (ry * upitch + rx) >> 1;
+          const float *vrow = veff_ext + ((size_t)K * p.EY + (J + ry)) * p.EX + (I + rx);
           const float2 zero2 = make_float2(0.f, 0.f);
           float2 win[W];
 #pragma unroll
           for (int q = -O; q < O; q++) {
-            const int zq = zb + q;
+            const int zq = rzb + q;
             win[q + O + 1] = (zq >= 0 && zq < nz) ? P2[rowP2 + min(max(zq, 0), nz - 1) * PS2] : zero2;
           }
-          // ring window: plane z + d lives in win[(z - zb + d + O + 1) % W]; the 13-step
+          // ring window: plane z + d lives in win[(z - rzb + d + O + 1) % W]; the 13-step
           // unroll keeps every index static so the window never moves between registers
-          for (int z0 = zb; z0 < ze; z0 += W) {
+          for (int z0 = rzb; z0 < rze; z0 += W) {
 #pragma unroll
             for (int s = 0; s < W; s++) {
               const int z = z0 + s;
-              if (z >= ze) break;
+              if (z >= rze) break;
               const int qn = z + O;
               win[s] = (qn < nz) ? P2[rowP2 + min(qn, nz - 1) * PS2] : zero2;
 #define WIN(dd) win[(s + (dd) + O + 1) % W]
@@ -595,7 +603,7 @@ __global__ void __launch_bounds__(512, 1)
               const float2 vc = WIN(0);
               float2 hz, hx, hy;
               hz.x = (p.cdiagf + vrow[z * VS]) * vc.x;
-              hz.y = (p.cdiagf + vrow[z * VS + phi]) * vc.y;
+              hz.y = (p.cdiagf + vrow[z * VS + rphi]) * vc.y;
               hx = zero2;
               hy = zero2;
   #pragma unroll
@@ -619,7 +627,7 @@ __global__ void __launch_bounds__(512, 1)
               float2 un;
               un.x = h.x - tbeta * uo.x;
               un.y = 0.f;
-              if (phi) {
+              if (rphi) {
                 a_acc += (vc.y * inv) * h.y;
                 un.y = h.y - tbeta * uo.y;
               }
@@ -628,6 +636,14 @@ __global__ void __launch_bounds__(512, 1)
 #undef WIN
             }
           }
+        };
+        if constexpr (WIDE) {
+          for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+            const int ty = t / npairs, tx = 2 * (t - ty * npairs);
+            pair_pass1(ty, tx, tx + 1 < nx ? 1 : 0, 0, nz);
+          }
+        } else if (pact) {
+          pair_pass1(py, pxc, phi, zb, ze);
         }
       } else {
         for (int y = y_begin; y < y_end; y++) {
@@ -739,24 +755,33 @@ __global__ void __launch_bounds__(512, 1)
       const T ta = T(a);
       T b_acc = T(0);
       if constexpr (PAIRED) {
-        if (pact) {
-          float2 *P2 = reinterpret_cast<float2 *>(P);
-          float2 *U2 = reinterpret_cast<float2 *>(U);
-          const int PS2 = PS >> 1, US2 = US >> 1;
-          const int rowP2 = (OFF + py * pitch + pxc) >> 1;
-          const int rowU2 = (py * upitch + pxc) >> 1;
-          for (int z = zb; z < ze; z++) {
+        float2 *P2 = reinterpret_cast<float2 *>(P);
+        float2 *U2 = reinterpret_cast<float2 *>(U);
+        const int PS2 = PS >> 1, US2 = US >> 1;
+        auto pair_pass2 = [&](const int ry, const int rx, const int rphi, const int rzb,
+                              const int rze) {
+          const int rowP2 = (OFF + ry * pitch + rx) >> 1;
+          const int rowU2 = (ry * upitch + rx) >> 1;
+          for (int z = rzb; z < rze; z++) {
             const float2 pv = P2[rowP2 + z * PS2];
             const float2 uv = U2[rowU2 + z * US2];
             float2 vk, w;
             vk.x = pv.x * inv;
-            vk.y = phi ? pv.y * inv : 0.f;
+            vk.y = rphi ? pv.y * inv : 0.f;
             w.x = uv.x - ta * vk.x;
-            w.y = phi ? uv.y - ta * vk.y : 0.f;
+            w.y = rphi ? uv.y - ta * vk.y : 0.f;
             P2[rowP2 + z * PS2] = w;
             U2[rowU2 + z * US2] = vk;
             b_acc += w.x * w.x + w.y * w.y;
           }
+        };
+        if constexpr (WIDE) {
+          for (int t = threadIdx.x; t < ntask; t += blockDim.x) {
+            const int ty = t / npairs, tx = 2 * (t - ty * npairs);
+            pair_pass2(ty, tx, tx + 1 < nx ? 1 : 0, 0, nz);
+          }
+        } else if (pact) {
+          pair_pass2(py, pxc, phi, zb, ze);
         }
       } else if (xin) {
         for (int y = y_begin; y < y_end; y++) {
@@ -799,13 +824,14 @@ __global__ void __launch_bounds__(512, 1)
   }
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, int MASK>
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool WIDE>
 cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t smem,
                            cudaStream_t s, const void *veff_ext, const ImageMeta *images,
                            const void *tables, void *u_scratch, void *proj_scratch, double *ab,
                            int *status) {
   constexpr bool YPAD = sizeof(T) == 4;  // FP32 pads y; FP64 does not fit padded
-  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD>;
+  static_assert(!WIDE || YPAD, "cubes wider than 32 points take the FP32 pair passes");
+  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD, WIDE>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<grid, block, smem, s>>>(p, (const T *)veff_ext, images, (const T *)tables, (T *)u_scratch,
@@ -813,17 +839,17 @@ cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t s
   return cudaGetLastError();
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM>
+template <typename T, bool FAITHFUL, bool U_SMEM, bool WIDE = false>
 cudaError_t launch_mask(int mask, const LanczosParams &p, int grid, int block, size_t smem,
                         cudaStream_t s, const void *veff_ext, const ImageMeta *images,
                         const void *tables, void *u_scratch, void *proj_scratch, double *ab,
                         int *status) {
   switch (mask) {
-    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    default: return launch_variant<T, FAITHFUL, U_SMEM, 15>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    default: return launch_variant<T, FAITHFUL, U_SMEM, 15, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
   }
 }
 

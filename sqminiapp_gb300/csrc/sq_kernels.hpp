@@ -11,6 +11,9 @@ namespace sq {
 
 constexpr int kMaxWarpsF32 = 16;  // one CTA per SM, 16 warps: 128 registers/thread
 constexpr int kMaxWarpsF64 = 16;  // FP64 register window needs up to 128 registers/thread
+// cubes wider than 32 points (FP32 only): one thread per (row, x pair), up to 18 warps, so a
+// 33^3 cube's 33 x 17 pairs run in one round at <= 112 registers/thread
+constexpr int kWideWarpsF32 = 18;
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;

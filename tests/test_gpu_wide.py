@@ -1,0 +1,85 @@
+"""GPU parity for cubes wider than 32 points: the uneven-batch workload's 32-atom cell (side
+17 bohr, 38^3 mesh, h = 0.4474 bohr, Rcut = 7 bohr, so 33^3 cubes; 40 Lanczos steps) through
+the FP32 wide kernel against the FP64 CPU oracle, and inside a mixed-cell batch.
+
+Tolerance: FP32 vectors (unit roundoff 6e-8) over 40 steps, the same 1e-4 relative bound on
+the quadrature moments of order <= 3 as the narrow FP32 kernel's parity tests; the first
+Lanczos coefficients to 1e-4 relative."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def wide_cell(tmp_path_factory):
+    from sqminiapp_gb300.decks import make_fcc_mg_deck
+    d = str(tmp_path_factory.mktemp("mg32wide"))
+    return make_fcc_mg_deck(d, "mg32w", ncell=2, h=0.45, rcut=7.0, n_qp=40, disp=0.2, seed=23)
+
+
+def _moments(lam, w):
+    return [np.sum(w * lam ** k, axis=1) for k in range(4)]
+
+
+def test_wide_cube_matches_oracle(wide_cell, oracle_mod):
+    from sqminiapp_gb300 import LSDFT
+    d, name, _ = wide_cell
+    o = oracle_mod.Oracle(d, name, faithful=False)
+    nodes = np.arange(0, o.n_nodes, 1409)
+    rng = np.random.default_rng(12)
+    veff = -0.25 + 0.05 * rng.standard_normal(o.n_nodes)
+    ref = o.nodes_and_weights(nodes=nodes, veff=veff, want_ab=True)
+    with LSDFT(d, name, faithful=False, precision=32) as eng:
+        assert eng.n_nodes == 38 ** 3
+        full = eng.NodesAndWeights_LSSGQ(veff=veff)
+        a, b = eng.lanczos_coefficients(eng.n_nodes)
+    np.testing.assert_allclose(a[nodes, :3], ref["a"][:, :3], rtol=1e-3, atol=1e-4)
+    np.testing.assert_allclose(b[nodes, :3], ref["b"][:, :3], rtol=1e-3, atol=1e-4)
+    for k, (g, e) in enumerate(zip(_moments(full["lambda"][nodes], full["weights"][nodes]),
+                                   _moments(ref["lambda"], ref["weights"]))):
+        err = np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e)))
+        assert err < 1e-4, "moment %d error %.3e" % (k, err)
+    for k in ("lambda_min", "lambda_max"):
+        np.testing.assert_allclose(full[k][nodes], ref[k], rtol=1e-3, atol=1e-3)
+    # every node of the full grid: weights sum to 1
+    assert np.allclose(np.sum(full["weights"], axis=1), 1.0, atol=1e-6)
+    assert np.all(np.isfinite(full["lambda"]))
+
+
+def test_wide_cube_rejects_fp64(wide_cell):
+    from sqminiapp_gb300 import LSDFT, SqError
+    d, name, _ = wide_cell
+    with pytest.raises(SqError) as e:
+        LSDFT(d, name, faithful=False, precision=64)
+    assert "FP32" in str(e.value)
+
+
+def test_wide_cube_in_mixed_batch(wide_cell, small_cell):
+    """A 33^3-cube cell beside a 9^3-cube cell in one batch submission: each gives its
+    single-cell result."""
+    import torch
+    from sqminiapp_gb300 import LSDFT, batch_nodes_and_weights
+    cells = [LSDFT(*wide_cell[:2], faithful=False, precision=32),
+             LSDFT(*small_cell[:2], faithful=False, precision=32)]
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(9)
+    veffs, outs, refs = [], [], []
+    for e in cells:
+        v = -0.2 + 0.05 * rng.standard_normal(e.n_nodes)
+        refs.append(e.NodesAndWeights_LSSGQ(veff=v))
+        veffs.append(torch.from_numpy(v).to(dev))
+        outs.append({k: torch.empty(s, dtype=torch.float64, device=dev) for k, s in
+                     (("lambda", (e.n_nodes, e.n_qp)), ("weights", (e.n_nodes, e.n_qp)),
+                      ("lambda_min", (e.n_nodes,)), ("lambda_max", (e.n_nodes,)))})
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    batch_nodes_and_weights(cells, [v.data_ptr() for v in veffs], None,
+                            [{k: t.data_ptr() for k, t in o.items()} for o in outs], stream)
+    torch.cuda.synchronize()
+    for o, r in zip(outs, refs):
+        lam, w = o["lambda"].cpu().numpy(), o["weights"].cpu().numpy()
+        for g, e in zip(_moments(lam, w), _moments(r["lambda"], r["weights"])):
+            assert np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e))) < 1e-4
+    for e in cells:
+        e.close()
