@@ -289,6 +289,10 @@ void build_engine(sq_handle *h) {
       sq::lanczos_smem_bytes(p, 4, true, faithful) <= (size_t)smem_optin)
     h->u_smem = true;
   h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
+  if (h->smem > (size_t)smem_optin && h->opt.precision == 64) {
+    p.pitch = p.nx;  // rows without zero columns; the kernel bounds-checks x instead
+    h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
+  }
   if (h->smem > (size_t)smem_optin)
     throw std::invalid_argument("cube of " + std::to_string(p.nx) + "x" + std::to_string(p.ny) +
                                 "x" + std::to_string(p.nz) +

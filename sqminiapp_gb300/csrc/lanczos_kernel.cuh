@@ -8,7 +8,8 @@
 //
 // Layout.  A persistent CTA (one per SM) owns one node at a time and keeps both Lanczos
 // vectors on chip:
-//   P  the stencil source, with 6 zero columns between rows (x) and, in FP32, 6 zero rows
+//   P  the stencil source, with 6 zero columns between rows (x; FP64 cubes too large for
+//      them drop the columns and bounds-check x instead) and, in FP32, 6 zero rows
 //      between consecutive z-planes and before the first (y): row -d of a plane is a zero
 //      row of the gap before it, row ny-1+d one of the gap after it, so no neighbour load
 //      needs a bounds check;
@@ -252,7 +253,7 @@ __device__ __forceinline__ void decode(const ImgView<T> &v, int t, int &lx, int 
   ly = row - lz * v.ey;
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD, bool WIDE>
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD, bool WIDE, bool XCLAMP>
 __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
     lanczos_kernel(const __grid_constant__ LanczosParams p, const T *__restrict__ veff_ext,
                    const ImageMeta *__restrict__ images, const T *__restrict__ tables,
@@ -667,7 +668,13 @@ __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
   #pragma unroll
             for (int d = 1; d <= O; d++) {
               h += Coef<T>::z(p, d) * (win[O - d] + win[O + d]);
-              h += Coef<T>::x(p, d) * (P[i - d] + P[i + d]);
+              if constexpr (XCLAMP) {  // no zero columns between rows: clamp, then drop
+                const T xm = P[xc - d >= 0 ? i - d : i];
+                const T xp = P[xc + d < nx ? i + d : i];
+                h += Coef<T>::x(p, d) * ((xc - d >= 0 ? xm : T(0)) + (xc + d < nx ? xp : T(0)));
+              } else {
+                h += Coef<T>::x(p, d) * (P[i - d] + P[i + d]);
+              }
               if constexpr (YPAD) {
                 h += Coef<T>::y(p, d) * (P[i - d * pitch] + P[i + d * pitch]);
               } else {  // rows outside the cube are zero: clamp the index, then drop the value
@@ -824,14 +831,15 @@ __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
   }
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool WIDE>
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool WIDE, bool XCLAMP>
 cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t smem,
                            cudaStream_t s, const void *veff_ext, const ImageMeta *images,
                            const void *tables, void *u_scratch, void *proj_scratch, double *ab,
                            int *status) {
   constexpr bool YPAD = sizeof(T) == 4;  // FP32 pads y; FP64 does not fit padded
   static_assert(!WIDE || YPAD, "cubes wider than 32 points take the FP32 pair passes");
-  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD, WIDE>;
+  static_assert(!XCLAMP || !YPAD, "x-clamped rows are an FP64 layout");
+  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD, WIDE, XCLAMP>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<grid, block, smem, s>>>(p, (const T *)veff_ext, images, (const T *)tables, (T *)u_scratch,
@@ -839,17 +847,17 @@ cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t s
   return cudaGetLastError();
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, bool WIDE = false>
+template <typename T, bool FAITHFUL, bool U_SMEM, bool WIDE = false, bool XCLAMP = false>
 cudaError_t launch_mask(int mask, const LanczosParams &p, int grid, int block, size_t smem,
                         cudaStream_t s, const void *veff_ext, const ImageMeta *images,
                         const void *tables, void *u_scratch, void *proj_scratch, double *ab,
                         int *status) {
   switch (mask) {
-    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    default: return launch_variant<T, FAITHFUL, U_SMEM, 15, WIDE>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    default: return launch_variant<T, FAITHFUL, U_SMEM, 15, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
   }
 }
 

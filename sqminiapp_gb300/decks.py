@@ -114,4 +114,9 @@ CONFIGS = {
     "mg108_h0.5_rc6.5_q40": dict(ncell=3, h=0.5, rcut=6.5, n_qp=40, disp=0.25,
                                  disp_kind="gaussian"),
     "mg500_h0.5_rc7_q50": dict(ncell=5, h=0.5, rcut=7.0, n_qp=50, disp=0.2),
+    # the uneven batch: three cells of different meshes, cube sizes (25^3, 33^3, 27^3) and
+    # Lanczos degrees in one submission
+    "uneven_a_mg4_h0.5_rc6_q30": dict(ncell=1, h=0.5, rcut=6.0, n_qp=30, disp=0.2),
+    "uneven_b_mg32_h0.45_rc7_q40": dict(ncell=2, h=0.45, rcut=7.0, n_qp=40, disp=0.2),
+    "uneven_c_mg108_h0.5_rc6.5_q50": dict(ncell=3, h=0.5, rcut=6.5, n_qp=50, disp=0.2),
 }

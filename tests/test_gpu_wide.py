@@ -1,6 +1,9 @@
-"""GPU parity for cubes wider than 32 points: the uneven-batch workload's 32-atom cell (side
-17 bohr, 38^3 mesh, h = 0.4474 bohr, Rcut = 7 bohr, so 33^3 cubes; 40 Lanczos steps) through
-the FP32 wide kernel against the FP64 CPU oracle, and inside a mixed-cell batch.
+"""GPU parity for the large-cube layouts.
+
+Cubes wider than 32 points: the uneven-batch workload's 32-atom cell (side 17 bohr, 38^3
+mesh, h = 0.4474 bohr, Rcut = 7 bohr, so 33^3 cubes; 40 Lanczos steps) through the FP32 wide
+kernel against the FP64 CPU oracle, and inside a mixed-cell batch.  FP64 cubes of 29^3: rows
+without zero columns.
 
 Tolerance: FP32 vectors (unit roundoff 6e-8) over 40 steps, the same 1e-4 relative bound on
 the quadrature moments of order <= 3 as the narrow FP32 kernel's parity tests; the first
@@ -83,3 +86,31 @@ def test_wide_cube_in_mixed_batch(wide_cell, small_cell):
             assert np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e))) < 1e-4
     for e in cells:
         e.close()
+
+
+def test_fp64_unpadded_rows_match_oracle(tmp_path_factory, oracle_mod):
+    """29^3 cubes (h = 0.5, Rcut = 7 bohr, the 500-atom workload's cube) in FP64: the x-padded
+    rows would need 235 KB of shared memory, so the kernel keeps rows of exactly 29 points and
+    bounds-checks x.  FP64 tolerance 1e-9 (summation order only)."""
+    from sqminiapp_gb300 import LSDFT
+    from sqminiapp_gb300.decks import make_fcc_mg_deck
+    d, name, _ = make_fcc_mg_deck(str(tmp_path_factory.mktemp("mg4rc7")), "mg4rc7", ncell=1,
+                                  h=0.5, rcut=7.0, n_qp=30, disp=0.2, seed=41)
+    o = oracle_mod.Oracle(d, name, faithful=False)
+    nodes = np.arange(0, o.n_nodes, 97)
+    rng = np.random.default_rng(13)
+    veff = -0.25 + 0.05 * rng.standard_normal(o.n_nodes)
+    ref = o.nodes_and_weights(nodes=nodes, veff=veff, want_ab=True)
+    with LSDFT(d, name, faithful=False, precision=64) as eng:
+        full = eng.NodesAndWeights_LSSGQ(veff=veff)
+        a, b = eng.lanczos_coefficients(eng.n_nodes)
+    np.testing.assert_allclose(a[nodes, :5], ref["a"][:, :5], rtol=1e-9, atol=1e-10)
+    np.testing.assert_allclose(b[nodes, :5], ref["b"][:, :5], rtol=1e-9, atol=1e-10)
+    for k, (g, e) in enumerate(zip(_moments(full["lambda"][nodes], full["weights"][nodes]),
+                                   _moments(ref["lambda"], ref["weights"]))):
+        err = np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e)))
+        assert err < 1e-9, "moment %d error %.3e" % (k, err)
+    with LSDFT(d, name, faithful=False, precision=32) as eng:
+        f32 = eng.NodesAndWeights_LSSGQ(veff=veff)
+    for g, e in zip(_moments(f32["lambda"], f32["weights"]), _moments(full["lambda"], full["weights"])):
+        assert np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e))) < 1e-4
