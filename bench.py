@@ -323,7 +323,11 @@ def run_ours(args):
                        "precision": "fp32 vectors, fp64 coefficients/quadrature/sums",
                        "step": "lanczos+quadrature of all nodes, fermi bisection, density, energy",
                        "l2": "flushed between steps (256 MiB write)",
-                       "lambda_f": res["lambda_f"], "e_band": res["e_band"]},
+                       "lambda_f": res["lambda_f"], "e_band": res["e_band"],
+                       "kernel_layout": {"flags": eng.info.kernel_layout,
+                                         "u_on_chip": bool(eng.info.kernel_u_on_chip),
+                                         "threads": eng.info.kernel_threads,
+                                         "smem_bytes": eng.info.kernel_smem_bytes}},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": float(peak[0]),
                          "unit": "TFLOP/s", "frac": achieved / float(peak[0]),
                          "traffic": traffic, "kernel": "lanczos_kernel<float>",

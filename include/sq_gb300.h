@@ -73,6 +73,14 @@ typedef struct sq_info {
   double n_electrons;   /* sum of valence electrons from the .ion file */
   int n_lm;             /* nonlocal (l,m) projectors per atom (union over types) */
   double proj_points_per_node;  /* mean over nodes of sum_images |projector box ∩ cube| */
+  /* Lanczos kernel configuration (0 from sq_describe_deck): vector layout flags (1 = zero rows
+   * between z-planes, FP32; 2 = cubes wider than 32 points, FP32; 4 = rows without zero
+   * columns, FP64), U on chip (1) or in global scratch (0), threads per CTA, shared memory
+   * bytes per CTA. */
+  int kernel_layout;
+  int kernel_u_on_chip;
+  int kernel_threads;
+  int kernel_smem_bytes;
 } sq_info;
 
 /* Read <deck_dir>/<name>.inpt/.ion/.relax and <deck_dir>/pseudopotential/<psd> and build the

@@ -31,7 +31,9 @@ class SqInfo(ctypes.Structure):
                 ("h", ctypes.c_double * 3), ("cell_half", ctypes.c_double * 3),
                 ("rcut", ctypes.c_double), ("beta", ctypes.c_double), ("dV", ctypes.c_double),
                 ("n_electrons", ctypes.c_double), ("n_lm", ctypes.c_int),
-                ("proj_points_per_node", ctypes.c_double)]
+                ("proj_points_per_node", ctypes.c_double), ("kernel_layout", ctypes.c_int),
+                ("kernel_u_on_chip", ctypes.c_int), ("kernel_threads", ctypes.c_int),
+                ("kernel_smem_bytes", ctypes.c_int)]
 
 
 class SqScfOptions(ctypes.Structure):

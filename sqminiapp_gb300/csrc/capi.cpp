@@ -178,6 +178,7 @@ void fill_info(sq_info &in, const sq::Deck &d, const sq::Setup &s, int max_img,
   for (int l = 0; l < 4; l++)
     if (mask & (1 << l)) in.n_lm += 2 * l + 1;
   in.proj_points_per_node = projector_points_per_node(s, d);
+  in.kernel_layout = in.kernel_u_on_chip = in.kernel_threads = in.kernel_smem_bytes = 0;
   for (int a = 0; a < 3; a++) {
     in.grid[a] = d.grid[a];
     in.cube[a] = s.cube[a];
@@ -285,12 +286,26 @@ void build_engine(sq_handle *h) {
   }
   const bool faithful = h->opt.faithful != 0;
   h->u_smem = false;
-  if (h->opt.precision == 32 && !wide &&
-      sq::lanczos_smem_bytes(p, 4, true, faithful) <= (size_t)smem_optin)
-    h->u_smem = true;
+  p.layout = 0;
+  if (h->opt.precision == 32) {
+    // first choice: y gaps and U on chip; then U on chip without the gaps (y bounds-checked);
+    // then y gaps with U in global scratch
+    const size_t optin = (size_t)smem_optin;
+    p.layout = sq::kLayoutYGap | (wide ? sq::kLayoutWide : 0);
+    if (!wide) {
+      if (sq::lanczos_smem_bytes(p, 4, true, faithful) <= optin) {
+        h->u_smem = true;
+      } else {
+        p.layout = 0;
+        if (sq::lanczos_smem_bytes(p, 4, true, faithful) <= optin) h->u_smem = true;
+        else p.layout = sq::kLayoutYGap;
+      }
+    }
+  }
   h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
   if (h->smem > (size_t)smem_optin && h->opt.precision == 64) {
     p.pitch = p.nx;  // rows without zero columns; the kernel bounds-checks x instead
+    p.layout = sq::kLayoutXClamp;
     h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
   }
   if (h->smem > (size_t)smem_optin)
@@ -299,7 +314,7 @@ void build_engine(sq_handle *h) {
                                 " does not fit in shared memory at this precision");
   h->grid = h->num_sms;
   {  // projector records pack the P and U indices of a cube point into 16 bits each
-    const long long pitch_rows = (h->opt.precision == 32) ? p.ny + sq::kStencilHalf : p.ny;
+    const long long pitch_rows = (p.layout & sq::kLayoutYGap) ? p.ny + sq::kStencilHalf : p.ny;
     const long long psize = (long long)sq::kStencilHalf * p.pitch + (long long)p.nz * pitch_rows * p.pitch;
     if (psize >= 65536 || (long long)p.upitch * p.ny * p.nz >= 65536)
       throw std::invalid_argument("truncated cube too large for 16-bit point indices");
@@ -338,6 +353,10 @@ void build_engine(sq_handle *h) {
   dev_alloc(&h->d_fermi_out, sizeof(double) * 4, "fermi out");
 
   fill_info(h->info, d, s, p.max_img, h->opt);
+  h->info.kernel_layout = p.layout;
+  h->info.kernel_u_on_chip = h->u_smem ? 1 : 0;
+  h->info.kernel_threads = h->block;
+  h->info.kernel_smem_bytes = (int)h->smem;
 }
 
 }  // namespace

@@ -46,7 +46,7 @@ int mask_nlm(int mask) {
 }
 
 size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bool faithful) {
-  const bool ypad = elem_size == 4;  // must match lk::launch_variant
+  const bool ypad = (p.layout & kLayoutYGap) != 0;
   const size_t ps = (size_t)(ypad ? p.ny + lk::O : p.ny) * p.pitch;
   const size_t off = ypad ? (size_t)lk::O * p.pitch : lk::O;
   const size_t psize = (off + p.nz * ps + 3) & ~size_t(3);
@@ -69,6 +69,11 @@ cudaError_t launch_lanczos_f64(int mask, bool faithful, const LanczosParams &p, 
                                int block, size_t smem, cudaStream_t s, const void *veff_ext,
                                const ImageMeta *images, const void *tables, void *u_scratch,
                                void *proj_scratch, double *ab, int *status);
+cudaError_t launch_lanczos_f32_nogap(int mask, bool faithful, const LanczosParams &p, int grid,
+                                     int block, size_t smem, cudaStream_t s,
+                                     const void *veff_ext, const ImageMeta *images,
+                                     const void *tables, void *u_scratch, void *proj_scratch,
+                                     double *ab, int *status);
 cudaError_t launch_lanczos_f32_wide(int mask, bool faithful, const LanczosParams &p, int grid,
                                     int block, size_t smem, cudaStream_t s, const void *veff_ext,
                                     const ImageMeta *images, const void *tables, void *u_scratch,
@@ -79,14 +84,22 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
                            const ImageMeta *images, const void *tables, void *u_scratch,
                            void *proj_scratch, double *ab, int *status) {
   const int mask = kernel_mask(p.union_mask);
-  if (p.nx > 32) {  // the wide instantiations: FP32 only, U in global scratch
-    if (precision != 32 || u_smem) return cudaErrorInvalidValue;
-    return launch_lanczos_f32_wide(mask, faithful, p, grid, block, smem, s, veff_ext, images,
-                                   tables, u_scratch, proj_scratch, ab, status);
-  }
-  if (precision == 32)
+  const bool gap = (p.layout & kLayoutYGap) != 0;
+  if (precision == 32) {
+    if (p.layout & kLayoutWide) {  // U in global scratch
+      if (!gap || u_smem) return cudaErrorInvalidValue;
+      return launch_lanczos_f32_wide(mask, faithful, p, grid, block, smem, s, veff_ext, images,
+                                     tables, u_scratch, proj_scratch, ab, status);
+    }
+    if (!gap) {  // U in shared memory
+      if (!u_smem) return cudaErrorInvalidValue;
+      return launch_lanczos_f32_nogap(mask, faithful, p, grid, block, smem, s, veff_ext, images,
+                                      tables, u_scratch, proj_scratch, ab, status);
+    }
     return launch_lanczos_f32(mask, faithful, u_smem, p, grid, block, smem, s, veff_ext, images,
                               tables, u_scratch, proj_scratch, ab, status);
+  }
+  if (gap || (p.layout & kLayoutWide) || u_smem) return cudaErrorInvalidValue;
   return launch_lanczos_f64(mask, faithful, p, grid, block, smem, s, veff_ext, images, tables,
                             u_scratch, proj_scratch, ab, status);
 }

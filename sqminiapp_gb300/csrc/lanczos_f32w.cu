@@ -9,8 +9,8 @@ cudaError_t launch_lanczos_f32_wide(int mask, bool faithful, const LanczosParams
                                     const ImageMeta *images, const void *tables, void *u_scratch,
                                     void *proj_scratch, double *ab, int *status) {
   if (faithful)
-    return lk::launch_mask<float, true, false, true>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-  return lk::launch_mask<float, false, false, true>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    return lk::launch_mask<float, true, false, kLayoutYGap | kLayoutWide>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+  return lk::launch_mask<float, false, false, kLayoutYGap | kLayoutWide>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
 }
 
 }  // namespace sq

@@ -13,12 +13,12 @@ cudaError_t launch_lanczos_f64(int mask, bool faithful, const LanczosParams &p, 
                                int block, size_t smem, cudaStream_t s, const void *veff_ext,
                                const ImageMeta *images, const void *tables, void *u_scratch,
                                void *proj_scratch, double *ab, int *status) {
-  if (p.pitch < p.nx + kStencilHalf)  // rows without zero columns (cubes of 29^3 and up)
+  if (p.layout & kLayoutXClamp)  // rows without zero columns (cubes of 29^3 and up)
     return launch_lanczos_f64_xclamp(mask, faithful, p, grid, block, smem, s, veff_ext, images,
                                      tables, u_scratch, proj_scratch, ab, status);
   if (faithful)
-    return lk::launch_mask<double, true, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-  return lk::launch_mask<double, false, false>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    return lk::launch_mask<double, true, false, 0>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+  return lk::launch_mask<double, false, false, 0>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
 }
 
 }  // namespace sq

@@ -10,8 +10,8 @@ cudaError_t launch_lanczos_f64_xclamp(int mask, bool faithful, const LanczosPara
                                       const void *tables, void *u_scratch, void *proj_scratch,
                                       double *ab, int *status) {
   if (faithful)
-    return lk::launch_mask<double, true, false, false, true>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-  return lk::launch_mask<double, false, false, false, true>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    return lk::launch_mask<double, true, false, kLayoutXClamp>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+  return lk::launch_mask<double, false, false, kLayoutXClamp>(mask, p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
 }
 
 }  // namespace sq

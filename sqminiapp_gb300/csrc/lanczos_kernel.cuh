@@ -253,8 +253,8 @@ __device__ __forceinline__ void decode(const ImgView<T> &v, int t, int &lx, int 
   ly = row - lz * v.ey;
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool YPAD, bool WIDE, bool XCLAMP>
-__global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, int LAYOUT>
+__global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 512, 1)
     lanczos_kernel(const __grid_constant__ LanczosParams p, const T *__restrict__ veff_ext,
                    const ImageMeta *__restrict__ images, const T *__restrict__ tables,
                    T *__restrict__ u_global, unsigned char *proj_scratch,
@@ -266,6 +266,8 @@ __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
   constexpr int ASTRIDE = FAITHFUL ? 1 : NLM;  // projector coefficients per atom slot
   const int nw = blockDim.x >> 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr bool YPAD = LAYOUT & kLayoutYGap, WIDE = LAYOUT & kLayoutWide,
+                 XCLAMP = LAYOUT & kLayoutXClamp;
   const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
   // P index of (x,y,z) = OFF + z*PS + y*pitch + x.  YPAD: O zero rows precede every z-plane
   // and follow the last, so y-neighbours need no bounds checks either.
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
   const int y_end = min(ny, y_begin + p.rows_per_warp);
   // FP32 vector passes: half-warp hw owns row py and a z-chunk [zb, ze); lane hl owns the x
   // pair (px, px+1) with px even.  pact = the pair has a cube point, phi = so does px+1.
-  constexpr bool PAIRED = YPAD;
+  constexpr bool PAIRED = sizeof(T) == 4;
   const int hw = threadIdx.x >> 4, hl = threadIdx.x & 15;
   const int nzs = max(1, (2 * nw) / ny);
   const int py = hw / nzs, zc = hw - (hw / nzs) * nzs;
@@ -610,7 +612,13 @@ __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
   #pragma unroll
               for (int d = 1; d <= O; d++) {
                 fma2s(hz, p.czf[d], add2(WIN(-d), WIN(d)));
-                fma2s(hy, p.cyf[d], add2(P2[i2 - d * pitch2], P2[i2 + d * pitch2]));
+                if constexpr (YPAD) {
+                  fma2s(hy, p.cyf[d], add2(P2[i2 - d * pitch2], P2[i2 + d * pitch2]));
+                } else {  // rows outside the cube are zero: clamp the index, then drop the value
+                  const float2 ym = P2[ry - d >= 0 ? i2 - d * pitch2 : i2];
+                  const float2 yp = P2[ry + d < ny ? i2 + d * pitch2 : i2];
+                  fma2s(hy, p.cyf[d], add2(ry - d >= 0 ? ym : zero2, ry + d < ny ? yp : zero2));
+                }
                 if (d % 2 == 0) {
                   fma2s(hx, p.cxf[d], add2(L[3 - d / 2], L[3 + d / 2]));
                 } else {
@@ -831,15 +839,16 @@ __global__ void __launch_bounds__(WIDE ? 32 * kWideWarpsF32 : 512, 1)
   }
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, bool WIDE, bool XCLAMP>
+template <typename T, bool FAITHFUL, bool U_SMEM, int MASK, int LAYOUT>
 cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t smem,
                            cudaStream_t s, const void *veff_ext, const ImageMeta *images,
                            const void *tables, void *u_scratch, void *proj_scratch, double *ab,
                            int *status) {
-  constexpr bool YPAD = sizeof(T) == 4;  // FP32 pads y; FP64 does not fit padded
-  static_assert(!WIDE || YPAD, "cubes wider than 32 points take the FP32 pair passes");
-  static_assert(!XCLAMP || !YPAD, "x-clamped rows are an FP64 layout");
-  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, YPAD, WIDE, XCLAMP>;
+  static_assert(!(LAYOUT & kLayoutWide) || (sizeof(T) == 4 && (LAYOUT & kLayoutYGap) && !U_SMEM),
+                "cubes wider than 32 points: FP32 pair passes, y gaps, U in global scratch");
+  static_assert(!(LAYOUT & kLayoutXClamp) || sizeof(T) == 8, "x-clamped rows are an FP64 layout");
+  static_assert(!(LAYOUT & kLayoutYGap) || sizeof(T) == 4, "y gaps are an FP32 layout");
+  auto k = lanczos_kernel<T, FAITHFUL, U_SMEM, MASK, LAYOUT>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<grid, block, smem, s>>>(p, (const T *)veff_ext, images, (const T *)tables, (T *)u_scratch,
@@ -847,17 +856,17 @@ cudaError_t launch_variant(const LanczosParams &p, int grid, int block, size_t s
   return cudaGetLastError();
 }
 
-template <typename T, bool FAITHFUL, bool U_SMEM, bool WIDE = false, bool XCLAMP = false>
+template <typename T, bool FAITHFUL, bool U_SMEM, int LAYOUT>
 cudaError_t launch_mask(int mask, const LanczosParams &p, int grid, int block, size_t smem,
                         cudaStream_t s, const void *veff_ext, const ImageMeta *images,
                         const void *tables, void *u_scratch, void *proj_scratch, double *ab,
                         int *status) {
   switch (mask) {
-    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
-    default: return launch_variant<T, FAITHFUL, U_SMEM, 15, WIDE, XCLAMP>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 3: return launch_variant<T, FAITHFUL, U_SMEM, 3, LAYOUT>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 5: return launch_variant<T, FAITHFUL, U_SMEM, 5, LAYOUT>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 6: return launch_variant<T, FAITHFUL, U_SMEM, 6, LAYOUT>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    case 7: return launch_variant<T, FAITHFUL, U_SMEM, 7, LAYOUT>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
+    default: return launch_variant<T, FAITHFUL, U_SMEM, 15, LAYOUT>(p, grid, block, smem, s, veff_ext, images, tables, u_scratch, proj_scratch, ab, status);
   }
 }
 

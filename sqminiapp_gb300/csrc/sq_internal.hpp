@@ -52,8 +52,8 @@ struct LanczosParams {
   int Nx, Ny, Nz;          // grid nodes per axis
   int EX, EY, EZ;          // padded Veff dims (N + 2*nh)
   int pitch;               // smem row pitch of the stencil vector: nx + kStencilHalf (even
-                           // in FP32), or nx for FP64 cubes that only fit without the
-                           // zero columns (x-neighbours then bounds-checked)
+                           // in FP32), or nx with kLayoutXClamp
+  int layout;              // kLayout* flags
   int upitch;              // row pitch of the elementwise vector U (nx, or nx + 1)
   int nqp;                 // Lanczos steps kept for the quadrature
   int n_images;

@@ -12,8 +12,13 @@ namespace sq {
 constexpr int kMaxWarpsF32 = 16;  // one CTA per SM, 16 warps: 128 registers/thread
 constexpr int kMaxWarpsF64 = 16;  // FP64 register window needs up to 128 registers/thread
 // cubes wider than 32 points (FP32 only): one thread per (row, x pair), up to 18 warps, so a
-// 33^3 cube's 33 x 17 pairs run in one round at <= 112 registers/thread
+// 33^3 cube's 33 x 17 pairs run in one round (96 registers/thread: 5 warps share a quarter SM)
 constexpr int kWideWarpsF32 = 18;
+
+// Layout of the Lanczos vectors on chip (LanczosParams::layout, bit flags):
+constexpr int kLayoutYGap = 1;    // FP32: 6 zero rows between z-planes (else y bounds-checked)
+constexpr int kLayoutWide = 2;    // FP32 cubes wider than 32 points: one thread per row pair
+constexpr int kLayoutXClamp = 4;  // FP64: rows without zero columns, x bounds-checked
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;

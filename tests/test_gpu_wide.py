@@ -2,8 +2,8 @@
 
 Cubes wider than 32 points: the uneven-batch workload's 32-atom cell (side 17 bohr, 38^3
 mesh, h = 0.4474 bohr, Rcut = 7 bohr, so 33^3 cubes; 40 Lanczos steps) through the FP32 wide
-kernel against the FP64 CPU oracle, and inside a mixed-cell batch.  FP64 cubes of 29^3: rows
-without zero columns.
+kernel against the FP64 CPU oracle, and inside a mixed-cell batch.  Cubes of 29^3: FP64 rows
+without zero columns, FP32 planes without zero rows between them (U on chip).
 
 Tolerance: FP32 vectors (unit roundoff 6e-8) over 40 steps, the same 1e-4 relative bound on
 the quadrature moments of order <= 3 as the narrow FP32 kernel's parity tests; the first
@@ -35,6 +35,8 @@ def test_wide_cube_matches_oracle(wide_cell, oracle_mod):
     ref = o.nodes_and_weights(nodes=nodes, veff=veff, want_ab=True)
     with LSDFT(d, name, faithful=False, precision=32) as eng:
         assert eng.n_nodes == 38 ** 3
+        assert eng.info.kernel_layout == 3 and eng.info.kernel_u_on_chip == 0  # y gaps, wide
+        assert eng.info.kernel_threads == 576
         full = eng.NodesAndWeights_LSSGQ(veff=veff)
         a, b = eng.lanczos_coefficients(eng.n_nodes)
     np.testing.assert_allclose(a[nodes, :3], ref["a"][:, :3], rtol=1e-3, atol=1e-4)
@@ -102,6 +104,7 @@ def test_fp64_unpadded_rows_match_oracle(tmp_path_factory, oracle_mod):
     veff = -0.25 + 0.05 * rng.standard_normal(o.n_nodes)
     ref = o.nodes_and_weights(nodes=nodes, veff=veff, want_ab=True)
     with LSDFT(d, name, faithful=False, precision=64) as eng:
+        assert eng.info.kernel_layout == 4  # rows without zero columns
         full = eng.NodesAndWeights_LSSGQ(veff=veff)
         a, b = eng.lanczos_coefficients(eng.n_nodes)
     np.testing.assert_allclose(a[nodes, :5], ref["a"][:, :5], rtol=1e-9, atol=1e-10)
@@ -111,6 +114,8 @@ def test_fp64_unpadded_rows_match_oracle(tmp_path_factory, oracle_mod):
         err = np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e)))
         assert err < 1e-9, "moment %d error %.3e" % (k, err)
     with LSDFT(d, name, faithful=False, precision=32) as eng:
+        # FP32 (y bounds-checked): no zero rows between z-planes, so that U fits on chip beside P
+        assert eng.info.kernel_layout == 0 and eng.info.kernel_u_on_chip == 1
         f32 = eng.NodesAndWeights_LSSGQ(veff=veff)
     for g, e in zip(_moments(f32["lambda"], f32["weights"]), _moments(full["lambda"], full["weights"])):
         assert np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e))) < 1e-4
