@@ -68,6 +68,15 @@ def parse_args():
     p.add_argument("--scf-model", default=WARM_START_MODEL,
                    help="learned start for the FP32 engine ('none' skips it); used when the cell "
                         "has the discretisation the model was trained at")
+    p.add_argument("--scf-learned", choices=["auto", "force"], default="auto",
+                   help="force: run the learned start on a cell of another discretisation too")
+    p.add_argument("--scf-fp64", choices=["full", "at-fp32-density"], default="full",
+                   help="FP64 leg: a full SCF from the atomic start, or one FP64 SCF iteration "
+                        "from the FP32 engine's converged density (free energy check for cells "
+                        "whose FP64 SCF takes too long)")
+    p.add_argument("--batch", choices=["none", "uneven"], default="none",
+                   help="uneven: time the three-cell mixed batch (one call per cell vs one "
+                        "batched submission)")
     return p.parse_args()
 
 
@@ -310,6 +319,9 @@ def run_ours(args):
     scf = None
     if rank == 0 and world == 1 and args.scf_config != "none":
         scf = scf_leg(args, local)
+    batch = None
+    if rank == 0 and world == 1 and args.batch != "none":
+        batch = batch_leg(args, local)
 
     if rank == 0:
         line = {
@@ -336,10 +348,63 @@ def run_ours(args):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 4 * args.steps,
             "clocks": clk, "wall_s": t_wall, "scf": scf,
         }
+        if batch is not None:
+            line["batch"] = batch
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
         dist.destroy_process_group()
+
+
+BATCH_CELLS = {"uneven": ["uneven_a_mg4_h0.5_rc6_q30", "uneven_b_mg32_h0.45_rc7_q40",
+                          "uneven_c_mg108_h0.5_rc6.5_q50"]}
+
+
+def batch_leg(args, local, reps=3):
+    """Several independent cells: one sq_nodes_and_weights_device call per cell in a row, and
+    one sq_batch_nodes_and_weights submission (FP32, constant Veff -0.2 Ha; device wall clock
+    over `reps` repetitions after one untimed run of each form)."""
+    import torch
+    from sqminiapp_gb300 import LSDFT, batch_nodes_and_weights
+    dev = torch.device("cuda", local)
+    cells, veffs, outs, names = [], [], [], BATCH_CELLS[args.batch]
+    for i, cfg_name in enumerate(names):
+        (d, n, _), _ = make_deck(cfg_name, i)
+        e = LSDFT(d, n, faithful=False, precision=32, device=local)
+        cells.append(e)
+        veffs.append(torch.full((e.n_nodes,), -0.2, dtype=torch.float64, device=dev))
+        outs.append({k: torch.empty(s, dtype=torch.float64, device=dev) for k, s in
+                     (("lambda", (e.n_nodes, e.n_qp)), ("weights", (e.n_nodes, e.n_qp)),
+                      ("lambda_min", (e.n_nodes,)), ("lambda_max", (e.n_nodes,)))})
+    st = torch.cuda.current_stream(dev).cuda_stream
+
+    def one(e, v, o):
+        e.nodes_and_weights_device(v.data_ptr(), 0.0, 0, e.n_nodes, o["lambda"].data_ptr(),
+                                   o["weights"].data_ptr(), o["lambda_min"].data_ptr(),
+                                   o["lambda_max"].data_ptr(), st)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize(dev)
+        return (time.perf_counter() - t0) / reps
+
+    per = [timed(lambda e=e, v=v, o=o: one(e, v, o)) for e, v, o in zip(cells, veffs, outs)]
+    seq = timed(lambda: [one(e, v, o) for e, v, o in zip(cells, veffs, outs)])
+    bat = timed(lambda: batch_nodes_and_weights(
+        cells, [v.data_ptr() for v in veffs], None,
+        [{k: t.data_ptr() for k, t in o.items()} for o in outs], st))
+    res = {"cells": [{"workload": nm, "nodes": e.n_nodes, "cube": list(e.cube), "n_qp": e.n_qp,
+                      "seconds": t, "nodes_per_s": e.n_nodes / t,
+                      "kernel_layout": e.info.kernel_layout}
+                     for nm, e, t in zip(names, cells, per)],
+           "one_call_per_cell_s": seq, "batched_s": bat}
+    for e in cells:
+        e.close()
+    return res
 
 
 def scf_leg(args, local):
@@ -349,11 +414,29 @@ def scf_leg(args, local):
     (deck_dir, name, meta), cfg = make_deck(args.scf_config, 0)
     out = {"workload": args.scf_config, "atoms": meta["natoms"], "start": "atomic superposition",
            "stop": "relative density residual < TOL_SCF (1e-6; 3e-5 floor for FP32 vectors)"}
-    for prec in [int(p) for p in args.scf_precisions.split(",") if p]:
+    precs = [int(p) for p in args.scf_precisions.split(",") if p]
+    if args.scf_fp64 == "at-fp32-density":
+        precs = [32] + [p for p in precs if p != 32]  # the FP32 density comes first
+    rho32 = None
+    for prec in precs:
         t0 = time.perf_counter()
         eng = LSDFT(deck_dir, name, faithful=False, precision=prec, device=local)
         eng.scf_begin()  # builds the pseudocharges / Poisson symbol once per geometry
         setup_s = time.perf_counter() - t0
+        if prec == 64 and args.scf_fp64 == "at-fp32-density":
+            # one FP64 iteration: the Harris-Foulkes free energy at the FP32 fixed point, equal
+            # to the FP64 SCF's to second order in the density difference
+            t0 = time.perf_counter()
+            r = eng.SCF_LSSGQ(rho_init=rho32, maxit=1, raise_on_maxit=False)
+            wall = time.perf_counter() - t0
+            out["fp64_at_fp32_density"] = {
+                "seconds": wall, "setup_seconds": setup_s,
+                "free_energy_per_atom": r["free_energy_per_atom"],
+                "density_residual": r["residual"],
+                "dF_per_atom_vs_fp32": abs(r["free_energy_per_atom"] -
+                                           out["fp32"]["free_energy_per_atom"])}
+            eng.close()
+            continue
         t0 = time.perf_counter()
         r = eng.SCF_LSSGQ(raise_on_maxit=False)
         wall = time.perf_counter() - t0
@@ -362,9 +445,12 @@ def scf_leg(args, local):
                               "free_energy_per_atom": r["free_energy_per_atom"],
                               "residual": r["residual"], "tol": r["tol"],
                               "sq_seconds": r["sq_ms"] / 1e3}
+        if prec == 32 and args.scf_fp64 == "at-fp32-density":
+            rho32 = eng.scf_density()[0].copy()
         eng.close()
     model_ok = (args.scf_model != "none" and os.path.exists(args.scf_model) and
-                all(cfg[k] == v for k, v in WARM_START_DISCRETISATION.items()))
+                (args.scf_learned == "force" or
+                 all(cfg[k] == v for k, v in WARM_START_DISCRETISATION.items())))
     if model_ok and 32 in [int(p) for p in args.scf_precisions.split(",") if p]:
         from sqminiapp_gb300 import WarmStartMLP
         model = WarmStartMLP(device=local, path=args.scf_model)
