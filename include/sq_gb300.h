@@ -48,6 +48,11 @@ typedef struct sq_options {
    * 64: FP64 everywhere. */
   int precision;
   int device;   /* CUDA device ordinal */
+  /* Per-node projector list format of the FP32 corrected operator: 0 automatic (compact when
+   * the full lists of all SMs would not stay in L2), 1 full (chi_lm and packed P|U indices per
+   * point), 2 compact (T_l per channel and box coordinates; chi_lm rebuilt while streaming).
+   * FP64 and the faithful operator always use the full format. */
+  int list_format;
 } sq_options;
 
 /* Engine facts after setup. */
@@ -75,8 +80,8 @@ typedef struct sq_info {
   double proj_points_per_node;  /* mean over nodes of sum_images |projector box ∩ cube| */
   /* Lanczos kernel configuration (0 from sq_describe_deck): vector layout flags (1 = zero rows
    * between z-planes, FP32; 2 = cubes wider than 32 points, FP32; 4 = rows without zero
-   * columns, FP64), U on chip (1) or in global scratch (0), threads per CTA, shared memory
-   * bytes per CTA. */
+   * columns, FP64; 8 = compact projector list), U on chip (1) or in global scratch (0),
+   * threads per CTA, shared memory bytes per CTA. */
   int kernel_layout;
   int kernel_u_on_chip;
   int kernel_threads;

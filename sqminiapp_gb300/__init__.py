@@ -46,13 +46,15 @@ class LSDFT:
     faithful=True keeps the reference operator with its quirks (shared projector
     coefficient per atom, pseudocharge-based image range); faithful=False (default) is the
     corrected operator.  precision=32 runs FP32 Lanczos vectors with FP64 recurrence
-    coefficients, quadrature and sums; precision=64 is FP64 throughout.
+    coefficients, quadrature and sums; precision=64 is FP64 throughout.  list_format picks
+    the FP32 corrected operator's projector-list records (0 automatic, 1 full chi_lm, 2
+    compact radial values; sq_options.list_format).
     """
 
-    def __init__(self, deck_dir, name, faithful=False, precision=32, device=0):
+    def __init__(self, deck_dir, name, faithful=False, precision=32, device=0, list_format=0):
         self._lib = lib()
         self._h = ctypes.c_void_p()
-        opt = SqOptions(int(bool(faithful)), int(precision), int(device))
+        opt = SqOptions(int(bool(faithful)), int(precision), int(device), int(list_format))
         check(self._lib.sq_create_from_deck(deck_dir.encode(), name.encode(), ctypes.byref(opt),
                                             ctypes.byref(self._h)), "sq_create_from_deck")
         info = SqInfo()

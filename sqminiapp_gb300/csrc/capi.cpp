@@ -170,6 +170,30 @@ double projector_points_per_node(const sq::Setup &s, const sq::Deck &d) {
   return total / ((double)d.grid[0] * d.grid[1] * d.grid[2]);
 }
 
+// Fraction of projector box points inside the FP32 support sphere, over all images: the
+// share of box points a per-node list keeps.
+double kept_fraction(const sq::Setup &s) {
+  double kept = 0.0, total = 0.0;
+  for (const sq::ImageMeta &im : s.images) {
+    const sq::TypeDesc &td = s.types[im.type];
+    const double r2 = td.support_r2_f32;
+    long long k = 0;
+    for (int z = 0; z < td.fz; z++) {
+      const double dz = im.oz + s.h[2] * z;
+      for (int y = 0; y < td.fy; y++) {
+        const double dy = im.oy + s.h[1] * y, ryz = dy * dy + dz * dz;
+        for (int x = 0; x < td.fx; x++) {
+          const double dx = im.ox + s.h[0] * x;
+          if (dx * dx + ryz <= r2) k++;
+        }
+      }
+    }
+    kept += (double)k;
+    total += (double)td.fx * td.fy * td.fz;
+  }
+  return total > 0.0 ? kept / total : 1.0;
+}
+
 void fill_info(sq_info &in, const sq::Deck &d, const sq::Setup &s, int max_img,
                const sq_options &opt) {
   int mask = 0;
@@ -302,6 +326,25 @@ void build_engine(sq_handle *h) {
       }
     }
   }
+  if (h->opt.precision == 32 && !faithful && h->opt.list_format != 1) {
+    // compact records when the full lists of all SMs (plus U slices in global scratch) would
+    // take more than 3/4 of the L2, or on request; only if the extra per-image data fits
+    bool compact = h->opt.list_format == 2;
+    if (!compact) {
+      int l2 = 0;
+      ck(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->opt.device), "L2 size");
+      const double kept = projector_points_per_node(s, d) * kept_fraction(s);
+      double bytes = (double)h->num_sms * kept *
+                     (double)sq::proj_record_bytes(4, false, p.union_mask, false);
+      if (!h->u_smem) bytes += (double)h->num_sms * 4.0 * p.upitch * p.ny * p.nz;
+      compact = bytes > 0.75 * (double)l2;
+    }
+    if (compact) {
+      sq::LanczosParams q = p;
+      q.layout |= sq::kLayoutCompact;
+      if (sq::lanczos_smem_bytes(q, 4, h->u_smem, faithful) <= (size_t)smem_optin) p = q;
+    }
+  }
   h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
   if (h->smem > (size_t)smem_optin && h->opt.precision == 64) {
     p.pitch = p.nx;  // rows without zero columns; the kernel bounds-checks x instead
@@ -323,7 +366,9 @@ void build_engine(sq_handle *h) {
   if (cap > (1LL << 31) - 1) throw std::invalid_argument("projector list too large");
   p.proj_cap = (int)cap;
   p.proj_bytes_per_cta =
-      (long long)((cap * sq::proj_record_bytes((int)h->elem, faithful, p.union_mask) + 255) & ~255LL);
+      (long long)((cap * sq::proj_record_bytes((int)h->elem, faithful, p.union_mask,
+                                               (p.layout & sq::kLayoutCompact) != 0) +
+                   255) & ~255LL);
 
   // device buffers
   dev_alloc(&h->d_images, sizeof(sq::ImageMeta) * s.images.size(), "images");
@@ -447,9 +492,11 @@ sq_status sq_create_from_deck(const char *deck_dir, const char *name, const sq_o
   *out = nullptr;
   sq_handle *h = new sq_handle();
   sq_status st = guarded([&] {
-    h->opt = opt ? *opt : sq_options{0, 32, 0};
+    h->opt = opt ? *opt : sq_options{0, 32, 0, 0};
     if (h->opt.precision != 32 && h->opt.precision != 64)
       return fail(SQ_BAD_INPUT, "precision must be 32 or 64");
+    if (h->opt.list_format < 0 || h->opt.list_format > 2)
+      return fail(SQ_BAD_INPUT, "list_format must be 0, 1 or 2");
     h->deck = sq::read_deck(deck_dir, name);
     h->setup = sq::build_setup(h->deck, h->opt.faithful != 0);
     build_engine(h);
@@ -471,7 +518,7 @@ sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful,
   return guarded([&] {
     sq::Deck d = sq::read_deck(deck_dir, name);
     sq::Setup s = sq::build_setup(d, faithful != 0);
-    sq_options opt{faithful, 0, 0};
+    sq_options opt{faithful, 0, 0, 0};
     *info = sq_info{};
     fill_info(*info, d, s, max_images_per_node(s, d), opt);
     for (size_t t = 0; t < s.types.size(); t++) {

@@ -32,7 +32,14 @@ int kernel_mask(int union_mask) {
   return (union_mask == 3 || union_mask == 5 || union_mask == 6 || union_mask == 7) ? union_mask : 15;
 }
 
-size_t proj_record_bytes(int elem_size, bool faithful, int union_mask) {
+size_t proj_record_bytes(int elem_size, bool faithful, int union_mask, bool compact) {
+  if (compact) {  // lk::ChanRec: channel values in one 8-byte word or whole 16-byte vectors
+    int nch = 0;
+    for (int l = 0; l < 4; l++)
+      if (kernel_mask(union_mask) & (1 << l)) nch++;
+    const size_t vb = (size_t)nch * elem_size;
+    return (vb <= 8 ? 8 : 16 * ((vb + 15) / 16)) + sizeof(unsigned);
+  }
   const int n = faithful ? 2 : mask_nlm(kernel_mask(union_mask));
   const int per_vec = 16 / elem_size;
   return (size_t)16 * ((n + per_vec - 1) / per_vec) + sizeof(unsigned);
@@ -58,6 +65,7 @@ size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bo
   b += sizeof(double) * 2 * (lk::kMaxWarps + 1) + sizeof(double) * 128;
   b += (size_t)elem_size * p.max_img * (cstride + astride);
   b += sizeof(int) * (8 * (size_t)p.max_img + 2) + sizeof(int) * 4;
+  if (p.layout & kLayoutCompact) b += (2 * sizeof(int) + 3 * (size_t)elem_size) * p.max_img;
   return b;
 }
 
@@ -74,6 +82,11 @@ cudaError_t launch_lanczos_f32_nogap(int mask, bool faithful, const LanczosParam
                                      const void *veff_ext, const ImageMeta *images,
                                      const void *tables, void *u_scratch, void *proj_scratch,
                                      double *ab, int *status);
+cudaError_t launch_lanczos_f32_compact(int mask, bool u_smem, const LanczosParams &p, int grid,
+                                       int block, size_t smem, cudaStream_t s,
+                                       const void *veff_ext, const ImageMeta *images,
+                                       const void *tables, void *u_scratch, void *proj_scratch,
+                                       double *ab, int *status);
 cudaError_t launch_lanczos_f32_wide(int mask, bool faithful, const LanczosParams &p, int grid,
                                     int block, size_t smem, cudaStream_t s, const void *veff_ext,
                                     const ImageMeta *images, const void *tables, void *u_scratch,
@@ -86,6 +99,11 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
   const int mask = kernel_mask(p.union_mask);
   const bool gap = (p.layout & kLayoutYGap) != 0;
   if (precision == 32) {
+    if (p.layout & kLayoutCompact) {  // corrected operator only
+      if (faithful) return cudaErrorInvalidValue;
+      return launch_lanczos_f32_compact(mask, u_smem, p, grid, block, smem, s, veff_ext, images,
+                                        tables, u_scratch, proj_scratch, ab, status);
+    }
     if (p.layout & kLayoutWide) {  // U in global scratch
       if (!gap || u_smem) return cudaErrorInvalidValue;
       return launch_lanczos_f32_wide(mask, faithful, p, grid, block, smem, s, veff_ext, images,
@@ -99,7 +117,7 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
     return launch_lanczos_f32(mask, faithful, u_smem, p, grid, block, smem, s, veff_ext, images,
                               tables, u_scratch, proj_scratch, ab, status);
   }
-  if (gap || (p.layout & kLayoutWide) || u_smem) return cudaErrorInvalidValue;
+  if (gap || (p.layout & (kLayoutWide | kLayoutCompact)) || u_smem) return cudaErrorInvalidValue;
   return launch_lanczos_f64(mask, faithful, p, grid, block, smem, s, veff_ext, images, tables,
                             u_scratch, proj_scratch, ab, status);
 }

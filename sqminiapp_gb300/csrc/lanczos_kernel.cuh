@@ -194,6 +194,41 @@ template <typename T, int N> struct ProjRec {
   }
 };
 
+// One record of the compact projector list (kLayoutCompact): the radial values T_l of the N
+// channels of the kernel's mask, in one 8-byte word when they fit, else in 16-byte vectors.
+template <typename T, int N> struct ChanRec {
+  static constexpr int n = N;
+  static constexpr bool word = N * (int)sizeof(T) <= 8;
+  using vec_t = typename std::conditional<
+      word, typename std::conditional<sizeof(T) == 4, float2, double>::type,
+      typename std::conditional<sizeof(T) == 4, float4, double2>::type>::type;
+  static constexpr int per_vec = (int)(sizeof(vec_t) / sizeof(T));
+  static constexpr int nvec = (N + per_vec - 1) / per_vec;
+  union Cast {
+    vec_t v;
+    T t[per_vec];
+  };
+  static __device__ __forceinline__ void store(vec_t *rec, int e, const T *v) {
+#pragma unroll
+    for (int j = 0; j < nvec; j++) {
+      Cast x;
+#pragma unroll
+      for (int s = 0; s < per_vec; s++) x.t[s] = j * per_vec + s < N ? v[j * per_vec + s] : T(0);
+      rec[(size_t)e * nvec + j] = x.v;
+    }
+  }
+  static __device__ __forceinline__ void load(const vec_t *rec, int e, T *c) {
+#pragma unroll
+    for (int j = 0; j < nvec; j++) {
+      Cast x;
+      x.v = rec[(size_t)e * nvec + j];
+#pragma unroll
+      for (int s = 0; s < per_vec; s++)
+        if (j * per_vec + s < N) c[j * per_vec + s] = x.t[s];
+    }
+  }
+};
+
 // Points per lane per batch of the projector-list streaming loops: 8 for records of up to
 // 16 bytes, fewer for wider records so the batch stays in registers.
 template <int BYTES> __host__ __device__ constexpr int stream_batch() { return BYTES <= 16 ? 8 : (BYTES <= 32 ? 4 : 2); }
@@ -260,8 +295,12 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
                    T *__restrict__ u_global, unsigned char *proj_scratch,
                    double *__restrict__ ab_out, int *__restrict__ status) {
   constexpr int NLM = Lm<MASK>::nlm;
-  using Rec = ProjRec<T, FAITHFUL ? 2 : NLM>;
-  constexpr int kStream = stream_batch<Rec::n * (int)sizeof(T)>();
+  constexpr bool COMPACT = LAYOUT & kLayoutCompact;
+  static_assert(!COMPACT || !FAITHFUL, "compact records carry the corrected operator's channels");
+  constexpr int NCH = (MASK & 1) + ((MASK >> 1) & 1) + ((MASK >> 2) & 1) + ((MASK >> 3) & 1);
+  using Rec = typename std::conditional<COMPACT, ChanRec<T, NCH>,
+                                        ProjRec<T, FAITHFUL ? 2 : NLM>>::type;
+  constexpr int kStream = stream_batch<Rec::nvec * (int)sizeof(typename Rec::vec_t)>();
   constexpr int CSTRIDE = FAITHFUL ? 2 : NLM;  // gather accumulators per atom slot
   constexpr int ASTRIDE = FAITHFUL ? 1 : NLM;  // projector coefficients per atom slot
   const int nw = blockDim.x >> 5;
@@ -297,6 +336,10 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
   cur += sizeof(T) * maxi * CSTRIDE;
   T *alpha = reinterpret_cast<T *>(cur);
   cur += sizeof(T) * maxi * ASTRIDE;
+  // compact records: per image of the node, its atom offset and P / U bases
+  T *cox = reinterpret_cast<T *>(cur), *coy = cox + maxi, *coz = coy + maxi;
+  int *cpb = reinterpret_cast<int *>(coz + maxi), *cub = cpb + maxi;
+  if constexpr (COMPACT) cur += (3 * sizeof(T) + 2 * sizeof(int)) * maxi;
   int *img = reinterpret_cast<int *>(cur);
   cur += sizeof(int) * maxi;
   int *slot = reinterpret_cast<int *>(cur);
@@ -340,6 +383,23 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
   const int pxc = px < nx ? px : ((nx - 1) & ~1);
   // WIDE: task t = (row t / npairs, pair t % npairs), all of z
   const int npairs = (nx + 1) >> 1, ntask = ny * npairs;
+
+  // compact records: chi_lm = P_lm(dx,dy,dz) T_l at a point, from the record's channel values
+  // tv (the same products the full list build stores); fn(rank of (l,m), chi_lm)
+  auto for_chi = [&](T dx, T dy, T dz, const T *tv, auto &&fn) {
+    int c = 0;
+    auto ch = [&](auto Lc) {
+      constexpr int L = decltype(Lc)::value;
+      if constexpr ((MASK >> L) & 1) {
+        const T t = tv[c++];
+        solid_harmonics<L, T>(dx, dy, dz, [&](int s, T ylm) { fn(Lm<MASK>::rank(s), ylm * t); });
+      }
+    };
+    ch(std::integral_constant<int, 0>{});
+    ch(std::integral_constant<int, 1>{});
+    ch(std::integral_constant<int, 2>{});
+    ch(std::integral_constant<int, 3>{});
+  };
 
   for (long long node = p.node_begin + blockIdx.x; node < p.node_end; node += gridDim.x) {
     const int I = (int)(node % p.Nx);
@@ -437,6 +497,15 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
     // chi_lm (or, faithful, sum_lm Gamma_l chi_lm and sum_lm chi_lm) and the packed P|U index.
     for (int kk = warp; kk < n_img; kk += nw) {
       const ImgView<T> v = load_view<T>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, OFF, PS);
+      if constexpr (COMPACT) {
+        if (lane == 0) {
+          cox[kk] = v.ox;
+          coy[kk] = v.oy;
+          coz[kk] = v.oz;
+          cpb[kk] = v.pbase;
+          cub[kk] = v.ubase;
+        }
+      }
       T gam[4];
       {
         const TypeDesc &td = p.types[slot_type[slot[kk]]];
@@ -453,7 +522,19 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
                 dz = v.oz + hz_of<T>(p) * T(lz);
         const bool ok = q < npts && dx * dx + dy * dy + dz * dz <= v.r2max;
         const unsigned m = __ballot_sync(0xffffffffu, ok);
-        if (ok) {
+        if constexpr (COMPACT) {
+          if (ok) {  // T_l of the mask's channels (0 where the type has none), box coordinates
+            const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
+            T out[Rec::n];
+            int chan = 0, c = 0;
+#pragma unroll
+            for (int l = 0; l < 4; l++)
+              if (MASK & (1 << l)) out[c++] = (v.chan_mask & (1 << l)) ? tb[(chan++) * v.fvol] : T(0);
+            const int e = pref[kk] + kept_n + __popc(m & ((1u << lane) - 1u));
+            Rec::store(rec, e, out);
+            ridx[e] = (unsigned)lx | ((unsigned)ly << 8) | ((unsigned)lz << 16);
+          }
+        } else if (ok) {
           const T *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
           T out[Rec::n];
 #pragma unroll
@@ -535,9 +616,17 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
         while (pos < r_end) {
           const int kend = min(r_end, koff[k + 1]);
           const int shift = pref[k] - koff[k];  // list position of kept point i is i + shift
-          T acc[Rec::n];
+          T acc[CSTRIDE];
 #pragma unroll
-          for (int s = 0; s < Rec::n; s++) acc[s] = T(0);
+          for (int s = 0; s < CSTRIDE; s++) acc[s] = T(0);
+          int pb = 0;
+          T ox = T(0), oy = T(0), oz = T(0);
+          if constexpr (COMPACT) {
+            pb = cpb[k];
+            ox = cox[k];
+            oy = coy[k];
+            oz = coz[k];
+          }
           // batches of kStream points per lane: all list loads of a batch are issued before
           // any is used (addresses clamped into the segment), so each warp keeps
           // 2*kStream L2 requests in flight
@@ -552,14 +641,21 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
             }
 #pragma unroll
             for (int u = 0; u < kStream; u++) {
-              const T val = (i0 + 32 * u < kend) ? P[ix[u] & 0xffffu] : T(0);
+              if constexpr (COMPACT) {
+                const int lx = ix[u] & 255u, ly = (ix[u] >> 8) & 255u, lz = ix[u] >> 16;
+                const T val = (i0 + 32 * u < kend) ? P[pb + lz * PS + ly * pitch + lx] : T(0);
+                for_chi(ox + hx_of<T>(p) * T(lx), oy + hy_of<T>(p) * T(ly),
+                        oz + hz_of<T>(p) * T(lz), c[u], [&](int r, T chi) { acc[r] += chi * val; });
+              } else {
+                const T val = (i0 + 32 * u < kend) ? P[ix[u] & 0xffffu] : T(0);
 #pragma unroll
-              for (int s = 0; s < Rec::n; s++) acc[s] += c[u][s] * val;
+                for (int s = 0; s < Rec::n; s++) acc[s] += c[u][s] * val;
+              }
             }
           }
           const int sl = slot[k];
 #pragma unroll
-          for (int s = 0; s < Rec::n; s++) {
+          for (int s = 0; s < CSTRIDE; s++) {
             const T r = warp_sum(acc[s]);
             if (lane == 0) atomicAdd(&cacc[sl * CSTRIDE + s], r);
           }
@@ -738,6 +834,14 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
           T coef[ASTRIDE];
 #pragma unroll
           for (int s = 0; s < ASTRIDE; s++) coef[s] = al[s];
+          int ub = 0;
+          T ox = T(0), oy = T(0), oz = T(0);
+          if constexpr (COMPACT) {
+            ub = cub[k];
+            ox = cox[k];
+            oy = coy[k];
+            oz = coz[k];
+          }
           for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
             T c[kStream][Rec::n];
             unsigned ix[kStream];
@@ -750,14 +854,23 @@ __global__ void __launch_bounds__((LAYOUT & kLayoutWide) ? 32 * kWideWarpsF32 : 
 #pragma unroll
             for (int u = 0; u < kStream; u++) {
               T val;
-              if constexpr (FAITHFUL) {
+              int ui;
+              if constexpr (COMPACT) {
+                const int lx = ix[u] & 255u, ly = (ix[u] >> 8) & 255u, lz = ix[u] >> 16;
+                ui = ub + (lz * ny + ly) * upitch + lx;
+                val = T(0);
+                for_chi(ox + hx_of<T>(p) * T(lx), oy + hy_of<T>(p) * T(ly),
+                        oz + hz_of<T>(p) * T(lz), c[u], [&](int r, T chi) { val += chi * coef[r]; });
+              } else if constexpr (FAITHFUL) {
+                ui = ix[u] >> 16;
                 val = c[u][1] * coef[0];
               } else {
+                ui = ix[u] >> 16;
                 val = T(0);
 #pragma unroll
                 for (int s = 0; s < Rec::n; s++) val += c[u][s] * coef[s];
               }
-              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u] >> 16], val);
+              if (i0 + 32 * u < kend) atomicAdd(&U[ui], val);
             }
           }
           pos = kend;

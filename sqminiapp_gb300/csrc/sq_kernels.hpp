@@ -19,6 +19,10 @@ constexpr int kWideWarpsF32 = 18;
 constexpr int kLayoutYGap = 1;    // FP32: 6 zero rows between z-planes (else y bounds-checked)
 constexpr int kLayoutWide = 2;    // FP32 cubes wider than 32 points: one thread per row pair
 constexpr int kLayoutXClamp = 4;  // FP64: rows without zero columns, x bounds-checked
+// FP32, corrected operator: the projector list holds T_l(r) per channel and the point's box
+// coordinates (12 B for s+p) instead of chi_lm and packed P|U indices (20 B); chi_lm is
+// rebuilt from the solid harmonics while streaming.  For lists that would not stay in L2.
+constexpr int kLayoutCompact = 8;
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;
@@ -32,8 +36,9 @@ int mask_nlm(int mask);
 
 size_t lanczos_smem_bytes(const LanczosParams &p, int elem_size, bool u_smem, bool faithful);
 
-// bytes of one record of the per-node projector list (values + packed P|U index)
-size_t proj_record_bytes(int elem_size, bool faithful, int union_mask);
+// bytes of one record of the per-node projector list (values + packed P|U index, or with
+// kLayoutCompact the channel values + packed box coordinates)
+size_t proj_record_bytes(int elem_size, bool faithful, int union_mask, bool compact = false);
 
 cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful, bool u_smem,
                            int grid, int block, size_t smem, cudaStream_t s, const void *veff_ext,
