@@ -104,6 +104,13 @@ sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful,
                            double *gamma, double *cutoff);
 sq_status sq_get_info(const sq_handle *h, sq_info *info);
 
+/* Host-only plan (no GPU touched): the info an engine built from this deck with these options
+ * would report on a device of num_sms SMs, smem_optin bytes of opt-in shared memory per block
+ * and l2_bytes of L2, including the kernel_* fields (on-chip layout, projector-list format,
+ * threads, shared memory).  A cell that fits no layout fails as sq_create_from_deck would. */
+sq_status sq_plan_kernel(const char *deck_dir, const char *name, const sq_options *opt,
+                         int num_sms, int smem_optin, int l2_bytes, sq_info *info);
+
 /* Per-node Lanczos + Gauss quadrature for nodes [node_begin, node_end) in the reference's
  * node order (z slowest, x fastest; src/lsdft_scf.cc:60-67).  Replaces
  * NodesAndWeights_LSSGQ (src/lsdft.h:132, called at src/main.cc:54), which loops

@@ -24,7 +24,10 @@ from .capi import SQ_OK, SqError, SqInfo, SqOptions, SqScfOptions, SqScfResult, 
 
 __all__ = ["LSDFT", "SqError", "library_path", "DECK_DIR", "lda_pw92", "Print_ElecDens",
            "Read_ElecDens", "Print_MinMaxLambda", "Read_MinMaxLambda", "WarmStartMLP",
-           "batch_nodes_and_weights"]
+           "batch_nodes_and_weights", "plan_kernel", "GB300_DEVICE"]
+
+# SM count, opt-in shared memory per block and L2 size of a GB300, for plan_kernel.
+GB300_DEVICE = {"num_sms": 152, "smem_optin": 232448, "l2_bytes": 126 * 1024 * 1024}
 
 DECK_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "decks")
 
@@ -307,6 +310,18 @@ class LSDFT:
               "sq_scf_get_fields")
         return {"b": arrs[0], "rho0": arrs[1], "phi": arrs[2], "vxc": arrs[3],
                 "e_self": sc[0], "e_self_ref": sc[1], "e_corr": sc[2], "b_total": sc[3]}
+
+
+def plan_kernel(deck_dir, name, faithful=False, precision=32, list_format=0, device=None):
+    """Host-only plan (sq_plan_kernel): the SqInfo an engine for this deck would report on a
+    device with the given properties (default GB300_DEVICE), kernel_* fields included."""
+    dev = dict(GB300_DEVICE, **(device or {}))
+    info = SqInfo()
+    opt = SqOptions(int(bool(faithful)), int(precision), 0, int(list_format))
+    check(lib().sq_plan_kernel(deck_dir.encode(), name.encode(), ctypes.byref(opt),
+                               int(dev["num_sms"]), int(dev["smem_optin"]), int(dev["l2_bytes"]),
+                               ctypes.byref(info)), "sq_plan_kernel")
+    return info
 
 
 def lda_pw92(rho):

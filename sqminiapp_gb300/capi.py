@@ -61,6 +61,9 @@ SIGNATURES = {
     "sq_describe_deck": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
                                         ctypes.POINTER(SqInfo), _dp, _dp]),
     "sq_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(SqInfo)]),
+    "sq_plan_kernel": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(SqOptions),
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.POINTER(SqInfo)]),
     "sq_nodes_and_weights": (ctypes.c_int, [_vp, _dp, _d, _l, _l, _dp, _dp, _dp, _dp]),
     "sq_nodes_and_weights_device": (ctypes.c_int, [_vp, _vp, _d, _l, _l, _vp, _vp, _vp, _vp, _vp]),
     "sq_sync_status": (ctypes.c_int, [_vp, _vp]),

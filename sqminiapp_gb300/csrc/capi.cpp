@@ -226,17 +226,12 @@ void fill_info(sq_info &in, const sq::Deck &d, const sq::Setup &s, int max_img,
   in.n_electrons = d.n_electrons;
 }
 
-void build_engine(sq_handle *h) {
+// Host part of the engine setup: the Lanczos kernel's parameters, on-chip layout, projector
+// list format, block and shared memory for a device with h->num_sms SMs, smem_optin bytes of
+// opt-in shared memory per block and l2_bytes of L2.  Touches no GPU.
+void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
   const sq::Deck &d = h->deck;
   const sq::Setup &s = h->setup;
-  ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
-  ck(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->opt.device), "sm count");
-  int smem_optin = 0;
-  ck(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->opt.device),
-     "smem optin");
-  ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
-  for (auto &e : h->ev) ck(cudaEventCreate(&e), "event");
-
   sq::LanczosParams &p = h->lp;
   p.nx = s.cube[0];
   p.ny = s.cube[1];
@@ -331,13 +326,11 @@ void build_engine(sq_handle *h) {
     // take more than 3/4 of the L2, or on request; only if the extra per-image data fits
     bool compact = h->opt.list_format == 2;
     if (!compact) {
-      int l2 = 0;
-      ck(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->opt.device), "L2 size");
       const double kept = projector_points_per_node(s, d) * kept_fraction(s);
       double bytes = (double)h->num_sms * kept *
                      (double)sq::proj_record_bytes(4, false, p.union_mask, false);
       if (!h->u_smem) bytes += (double)h->num_sms * 4.0 * p.upitch * p.ny * p.nz;
-      compact = bytes > 0.75 * (double)l2;
+      compact = bytes > 0.75 * (double)l2_bytes;
     }
     if (compact) {
       sq::LanczosParams q = p;
@@ -369,6 +362,25 @@ void build_engine(sq_handle *h) {
       (long long)((cap * sq::proj_record_bytes((int)h->elem, faithful, p.union_mask,
                                                (p.layout & sq::kLayoutCompact) != 0) +
                    255) & ~255LL);
+  fill_info(h->info, d, s, p.max_img, h->opt);
+  h->info.kernel_layout = p.layout;
+  h->info.kernel_u_on_chip = h->u_smem ? 1 : 0;
+  h->info.kernel_threads = h->block;
+  h->info.kernel_smem_bytes = (int)h->smem;
+}
+
+void build_engine(sq_handle *h) {
+  ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+  ck(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->opt.device), "sm count");
+  int smem_optin = 0, l2 = 0;
+  ck(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->opt.device),
+     "smem optin");
+  ck(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->opt.device), "L2 size");
+  plan_engine(h, smem_optin, l2);
+  ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
+  for (auto &e : h->ev) ck(cudaEventCreate(&e), "event");
+  const sq::Setup &s = h->setup;
+  const sq::LanczosParams &p = h->lp;
 
   // device buffers
   dev_alloc(&h->d_images, sizeof(sq::ImageMeta) * s.images.size(), "images");
@@ -396,12 +408,6 @@ void build_engine(sq_handle *h) {
             "fermi scratch");
   dev_alloc(&h->d_bar, sizeof(unsigned) * 2, "barrier");
   dev_alloc(&h->d_fermi_out, sizeof(double) * 4, "fermi out");
-
-  fill_info(h->info, d, s, p.max_img, h->opt);
-  h->info.kernel_layout = p.layout;
-  h->info.kernel_u_on_chip = h->u_smem ? 1 : 0;
-  h->info.kernel_threads = h->block;
-  h->info.kernel_smem_bytes = (int)h->smem;
 }
 
 }  // namespace
@@ -527,6 +533,27 @@ sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful,
       if (cutoff)
         for (int a = 0; a < 3; a++) cutoff[3 * t + a] = s.pseudocharge_cutoff[3 * t + a];
     }
+    return SQ_OK;
+  });
+}
+
+sq_status sq_plan_kernel(const char *deck_dir, const char *name, const sq_options *opt,
+                         int num_sms, int smem_optin, int l2_bytes, sq_info *info) {
+  if (!deck_dir || !name || !opt || !info) return fail(SQ_BAD_INPUT, "null argument");
+  if (num_sms <= 0 || smem_optin <= 0 || l2_bytes <= 0)
+    return fail(SQ_BAD_INPUT, "device properties must be positive");
+  if (opt->precision != 32 && opt->precision != 64)
+    return fail(SQ_BAD_INPUT, "precision must be 32 or 64");
+  if (opt->list_format < 0 || opt->list_format > 2)
+    return fail(SQ_BAD_INPUT, "list_format must be 0, 1 or 2");
+  sq_handle h;  // host fields only: no device buffer, stream or event is created
+  return guarded([&] {
+    h.opt = *opt;
+    h.deck = sq::read_deck(deck_dir, name);
+    h.setup = sq::build_setup(h.deck, opt->faithful != 0);
+    h.num_sms = num_sms;
+    plan_engine(&h, smem_optin, l2_bytes);
+    *info = h.info;
     return SQ_OK;
   });
 }

@@ -1,0 +1,67 @@
+"""The engine's choice of Lanczos-kernel layout per cell, planned on the host (sq_plan_kernel,
+the same code sq_create_from_deck runs before it allocates): on-chip layout flags, U on chip
+or in global scratch, projector-list format, threads and shared memory on a GB300."""
+import pytest
+
+from sqminiapp_gb300 import GB300_DEVICE, SqError, plan_kernel
+from sqminiapp_gb300.decks import CONFIGS, make_fcc_mg_deck
+
+YGAP, WIDE, XCLAMP, COMPACT = 1, 2, 4, 8
+
+
+@pytest.fixture(scope="module")
+def decks(tmp_path_factory):
+    out = {}
+    for name in ("mg32_h0.5_rc6.5_q40", "mg500_h0.5_rc7_q50", "uneven_b_mg32_h0.45_rc7_q40",
+                 "uneven_a_mg4_h0.5_rc6_q30"):
+        d = str(tmp_path_factory.mktemp(name))
+        out[name] = make_fcc_mg_deck(d, "c", **CONFIGS[name])[:2]
+    return out
+
+
+def _plan(decks, name, **kw):
+    return plan_kernel(*decks[name], **kw)
+
+
+def test_fp32_layouts(decks):
+    smem_max = GB300_DEVICE["smem_optin"]
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40")  # 27^3: y gaps, U on chip, 14 warps, full list
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP, 1, 448)
+    p = _plan(decks, "uneven_a_mg4_h0.5_rc6_q30")  # 25^3
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 1)
+    p = _plan(decks, "mg500_h0.5_rc7_q50")  # 29^3: U on chip only without the y gaps
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (0, 1)
+    p = _plan(decks, "uneven_b_mg32_h0.45_rc7_q40")  # 33^3: wide, U in L2, compact list
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP | WIDE | COMPACT, 0, 576)
+    for name in decks:
+        assert 0 < _plan(decks, name).kernel_smem_bytes <= smem_max
+
+
+def test_list_format_option(decks):
+    assert _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", list_format=1).kernel_layout == YGAP | WIDE
+    assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2).kernel_layout == YGAP | COMPACT
+    # the faithful operator and FP64 keep the full records
+    assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2, faithful=True).kernel_layout == YGAP
+    assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2, precision=64).kernel_layout == 0
+    # a small L2 turns the automatic choice to compact records
+    small = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"l2_bytes": 16 << 20})
+    assert small.kernel_layout == YGAP | COMPACT
+    with pytest.raises(SqError):
+        _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=3)
+
+
+def test_fp64_layouts(decks):
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40", precision=64)
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (0, 0, 448)
+    p = _plan(decks, "mg500_h0.5_rc7_q50", precision=64)  # 29^3: rows without zero columns
+    assert p.kernel_layout == XCLAMP
+    with pytest.raises(SqError) as e:  # 33^3 in FP64 fits no single-CTA layout
+        _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", precision=64)
+    assert "FP32" in str(e.value)
+
+
+def test_smaller_shared_memory_moves_u_off_chip(decks):
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 160 * 1024})
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 0)
+    with pytest.raises(SqError):
+        _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 64 * 1024})
