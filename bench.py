@@ -74,6 +74,10 @@ def parse_args():
                    help="FP64 leg: a full SCF from the atomic start, or one FP64 SCF iteration "
                         "from the FP32 engine's converged density (free energy check for cells "
                         "whose FP64 SCF takes too long)")
+    p.add_argument("--scf-mixing", type=float, default=0.5,
+                   help="mixing parameter of every time-to-SCF leg (0: the deck's)")
+    p.add_argument("--scf-kerker", type=float, default=2.0,
+                   help="Kerker k_TF (1/bohr) of every time-to-SCF leg (0: the engine's 1.0)")
     p.add_argument("--batch", choices=["none", "uneven"], default="none",
                    help="uneven: time the three-cell mixed batch (one call per cell vs one "
                         "batched submission)")
@@ -414,6 +418,9 @@ def scf_leg(args, local):
     (deck_dir, name, meta), cfg = make_deck(args.scf_config, 0)
     out = {"workload": args.scf_config, "atoms": meta["natoms"], "start": "atomic superposition",
            "stop": "relative density residual < TOL_SCF (1e-6; 3e-5 floor for FP32 vectors)"}
+    # the same mixing for every leg: the deck's history and Pulay period, this parameter and k_TF
+    mixing = {"mixing_parameter": args.scf_mixing or None, "kerker_ktf": args.scf_kerker or None}
+    out["mixing"] = {"parameter": args.scf_mixing or "deck", "kerker_ktf": args.scf_kerker or 1.0}
     precs = [int(p) for p in args.scf_precisions.split(",") if p]
     if args.scf_fp64 == "at-fp32-density":
         precs = [32] + [p for p in precs if p != 32]  # the FP32 density comes first
@@ -427,7 +434,7 @@ def scf_leg(args, local):
             # one FP64 iteration: the Harris-Foulkes free energy at the FP32 fixed point, equal
             # to the FP64 SCF's to second order in the density difference
             t0 = time.perf_counter()
-            r = eng.SCF_LSSGQ(rho_init=rho32, maxit=1, raise_on_maxit=False)
+            r = eng.SCF_LSSGQ(rho_init=rho32, maxit=1, raise_on_maxit=False, **mixing)
             wall = time.perf_counter() - t0
             out["fp64_at_fp32_density"] = {
                 "seconds": wall, "setup_seconds": setup_s,
@@ -438,7 +445,7 @@ def scf_leg(args, local):
             eng.close()
             continue
         t0 = time.perf_counter()
-        r = eng.SCF_LSSGQ(raise_on_maxit=False)
+        r = eng.SCF_LSSGQ(raise_on_maxit=False, **mixing)
         wall = time.perf_counter() - t0
         out["fp%d" % prec] = {"seconds": wall, "setup_seconds": setup_s,
                               "iterations": r["iterations"], "converged": bool(r["converged"]),
@@ -457,7 +464,7 @@ def scf_leg(args, local):
         eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local)
         eng.scf_begin()
         t0 = time.perf_counter()
-        r = eng.SCF_LSSGQ(raise_on_maxit=False, model=model)  # descriptors + MLP inside
+        r = eng.SCF_LSSGQ(raise_on_maxit=False, model=model, **mixing)  # descriptors + MLP inside
         wall = time.perf_counter() - t0
         out["fp32_learned"] = {"seconds": wall, "iterations": r["iterations"],
                                "converged": bool(r["converged"]),

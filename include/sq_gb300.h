@@ -221,7 +221,7 @@ typedef struct sq_scf_options {
   int pulay_frequency;      /* <= 0: PULAY_FREQUENCY */
   double fermi_tol;         /* bisection tolerance on lambda_f; <= 0: 1e-12 */
   double kerker_ktf;        /* Kerker preconditioner k_TF (1/bohr) of the mixing: > 0 that value,
-                               0 the default 2.0 (the reference mixes preconditioned,
+                               0 the default 1.0 (the reference mixes preconditioned,
                                src/lsdft_readfiles.cc:102), < 0 no preconditioner */
   int cuda_graph;           /* 1: from the second iteration on, replay one captured CUDA graph
                                of the iteration's device part (Poisson, potential, Lanczos,

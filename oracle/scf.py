@@ -225,8 +225,8 @@ def periodic_pulay_step(x, f, state, k, mix, history, every, precond=None):
     return np.maximum(xbar + mix * fbar, 0.0)
 
 
-def scf(o: Oracle, fields=None, tol=1e-6, maxit=100, mix=0.5, history=7, pulay_every=2,
-        rho_init=None, nthreads=None, fermi_tol=1e-12, k_tf=2.0):
+def scf(o: Oracle, fields=None, tol=1e-6, maxit=100, mix=0.3, history=7, pulay_every=2,
+        rho_init=None, nthreads=None, fermi_tol=1e-12, k_tf=1.0):
     """SCF with the oracle's per-node Lanczos/quadrature (corrected operator expected).
     k_tf > 0: Kerker-preconditioned mixing with that Thomas-Fermi wave vector (1/bohr);
     k_tf <= 0: unpreconditioned.  Returns the last iteration's quantities and the history of

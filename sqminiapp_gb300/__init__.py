@@ -217,7 +217,7 @@ class LSDFT:
         rho_init: None (superposition of atomic valence densities) or a host density over the
         FD grid.  None for any option takes the deck's value (TOL_SCF, MAXIT_SCF,
         MIXING_PARAMETER, MIXING_HISTORY, PULAY_FREQUENCY); kerker_ktf None/0 = Kerker with
-        k_TF = 2/bohr, negative = unpreconditioned mixing.  Returns the result dict of the
+        k_TF = 1/bohr, negative = unpreconditioned mixing.  Returns the result dict of the
         last iteration with the per-iteration history of free energy and residual."""
         opt = self._scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency,
                                 fermi_tol, kerker_ktf, cuda_graph)

@@ -48,9 +48,10 @@ constexpr int kMaxSums = (kMaxHistory + 1) * (kMaxHistory + 2) / 2;
 // (measured on 4-atom Mg cells at h = 0.5 and 0.85); the FP32 engine never asks for less.
 // At that residual its free energy is within 1e-6 Ha/atom of the FP64 engine's.
 constexpr double kFp32ResidualFloor = 3e-5;
-// Default Kerker wave vector (1/bohr).  Of 0.7, 1, 1.5, 2 and 3 on the 32- and 108-atom Mg
-// cells (h = 0.5, 1000 K, mixing 0.3-0.7), 2 converged in the fewest iterations.
-constexpr double kKerkerKtf = 2.0;
+// Default Kerker wave vector (1/bohr).  Larger cells converge faster with stronger damping of
+// their long wavelengths (k_TF 2 with mixing 0.5 on 32 and 108 Mg atoms), the 4-atom cell
+// with less (k_TF 1, mixing 0.3); callers choose per cell through sq_scf_options.
+constexpr double kKerkerKtf = 1.0;
 
 void ckfft(cufftResult r, const char *what) {
   if (r != CUFFT_SUCCESS) throw CudaError(std::string(what) + ": cuFFT error " + std::to_string((int)r));

@@ -58,7 +58,7 @@ def fcc_positions(ncell, a=A_MG):
 
 def make_fcc_mg_deck(out_dir, name, ncell, h, rcut, n_qp, disp=0.1, disp_kind="uniform",
                      seed=DEFAULT_SEED, lloc=2, temperature_k=1000.0, reference_layout=False,
-                     mixing=0.5, mixing_history=7, tol_scf=1e-6):
+                     mixing=0.3, mixing_history=7, tol_scf=1e-6):
     """Write an FCC Mg deck; returns (out_dir, name, info dict)."""
     L = A_MG * ncell
     N = int(round(L / h))
