@@ -27,7 +27,9 @@
 // the real solid harmonics).  Every Lanczos step then streams that list twice, cut into
 // equal per-warp ranges: the gather accumulates c_lm = <chi_lm, P> per lane and adds the
 // shuffle-reduced sums into the atom's slot with shared atomics when a range leaves an
-// image; the scatter adds sum_lm chi_lm alpha_lm into U with shared atomics.
+// image; the scatter adds sum_lm chi_lm alpha_lm into U with shared atomics.  Compact lists
+// (kLayoutCompact) store T_l(r) per channel and the point's box coordinates instead, and the
+// stream rebuilds chi_lm and the P/U indices from per-image data kept in shared memory.
 //
 // Recurrence (reference scf.cc:119-147, same quantities, fused passes):
 //   P = b_{k-1} v_k (unnormalised), U = v_{k-1};
