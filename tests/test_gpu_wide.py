@@ -140,3 +140,63 @@ def test_compact_list_matches_full(which, wide_cell, small_cell):
     for g, e in zip(_moments(out[2]["lambda"], out[2]["weights"]),
                     _moments(out[1]["lambda"], out[1]["weights"])):
         assert np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e))) < 1e-5
+
+
+def _parity(eng_out, ref, nodes, tol):
+    for k, (g, e) in enumerate(zip(_moments(eng_out["lambda"][nodes], eng_out["weights"][nodes]),
+                                   _moments(ref["lambda"], ref["weights"]))):
+        err = np.max(np.abs(g - e) / np.maximum(1.0, np.abs(e)))
+        assert err < tol, "moment %d error %.3e" % (k, err)
+
+
+def test_fp32_u_in_global_scratch_31cube(tmp_path_factory, oracle_mod):
+    """31^3 cubes (h = 0.5, Rcut = 7.5 bohr): the FP32 kernel keeps P with its y gaps on chip
+    and U in global scratch; FP64 fits no single-CTA layout there."""
+    from sqminiapp_gb300 import LSDFT, SqError
+    from sqminiapp_gb300.decks import make_fcc_mg_deck
+    d, name, _ = make_fcc_mg_deck(str(tmp_path_factory.mktemp("mg4rc75")), "mg4rc75", ncell=1,
+                                  h=0.5, rcut=7.5, n_qp=30, disp=0.2, seed=43)
+    o = oracle_mod.Oracle(d, name, faithful=False)
+    nodes = np.arange(0, o.n_nodes, 131)
+    veff = np.full(o.n_nodes, -0.2)
+    ref = o.nodes_and_weights(nodes=nodes, veff=veff)
+    with LSDFT(d, name, faithful=False, precision=32) as eng:
+        assert eng.cube == (31, 31, 31)
+        assert eng.info.kernel_layout & 7 == 1 and eng.info.kernel_u_on_chip == 0
+        got = eng.NodesAndWeights_LSSGQ(veff=veff)
+    _parity(got, ref, nodes, 1e-4)
+    with pytest.raises(SqError) as e:
+        LSDFT(d, name, faithful=False, precision=64)
+    assert "shared memory" in str(e.value)
+
+
+@pytest.mark.parametrize("precision,tol", [(32, 1e-4), (64, 1e-9)])
+def test_faithful_operator_on_large_cube_layouts(precision, tol, tmp_path_factory, oracle_mod):
+    """The reference's shared-slot operator through the 29^3 layouts (FP32 planes without y
+    gaps, FP64 rows without zero columns) against the faithful oracle."""
+    from sqminiapp_gb300 import LSDFT
+    from sqminiapp_gb300.decks import make_fcc_mg_deck
+    d, name, _ = make_fcc_mg_deck(str(tmp_path_factory.mktemp("mg4rc7f")), "mg4rc7f", ncell=1,
+                                  h=0.5, rcut=7.0, n_qp=30, disp=0.2, seed=41)
+    o = oracle_mod.Oracle(d, name, faithful=True)
+    nodes = np.arange(0, o.n_nodes, 163)
+    veff = np.full(o.n_nodes, -0.2)
+    ref = o.nodes_and_weights(nodes=nodes, veff=veff)
+    with LSDFT(d, name, faithful=True, precision=precision) as eng:
+        assert eng.info.kernel_layout == (0 if precision == 32 else 4)
+        got = eng.NodesAndWeights_LSSGQ(veff=veff)
+    _parity(got, ref, nodes, tol)
+
+
+def test_faithful_operator_on_wide_cube(wide_cell, oracle_mod):
+    """The shared-slot operator on the 33^3 cell (FP32 WIDE, full records)."""
+    from sqminiapp_gb300 import LSDFT
+    d, name, _ = wide_cell
+    o = oracle_mod.Oracle(d, name, faithful=True)
+    nodes = np.arange(0, o.n_nodes, 2417)
+    veff = np.full(o.n_nodes, -0.2)
+    ref = o.nodes_and_weights(nodes=nodes, veff=veff)
+    with LSDFT(d, name, faithful=True, precision=32) as eng:
+        assert eng.info.kernel_layout == 3
+        got = eng.NodesAndWeights_LSSGQ(veff=veff)
+    _parity(got, ref, nodes, 1e-4)
