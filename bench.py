@@ -61,6 +61,9 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--max-nodes", type=int, default=0,
                    help="process only the first N nodes per step (profiling of small cases)")
+    p.add_argument("--list-format", type=int, choices=[0, 1, 2], default=0,
+                   help="projector-list records of the main workload: 0 automatic, 1 full, "
+                        "2 compact")
     p.add_argument("--scf-config", default=SCF_WORKLOAD,
                    help="cell of the time-to-SCF leg ('none' skips it)")
     p.add_argument("--scf-precisions", default="32,64",
@@ -217,7 +220,8 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl")
     (deck_dir, name, meta), cfg = make_deck(args.config, rank)
-    eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local)
+    eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local,
+                list_format=args.list_format)
     n, q = eng.n_nodes, eng.n_qp
     if args.max_nodes > 0:
         n = min(n, args.max_nodes)
