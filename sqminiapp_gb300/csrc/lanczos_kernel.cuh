@@ -86,18 +86,19 @@ template <typename T> __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Sum of one double per thread over the CTA (nw warps), behind one barrier: every thread adds
-// the nw warp sums itself, in the same order, so all threads hold the same value.  red holds
-// kMaxWarps+1 doubles; a caller alternates two buffers so that a barrier separates the reads
-// of one sum from the writes of the next sum into the same buffer.
+// Sum of one double per thread over the CTA (nw warps); red holds kMaxWarps+1 doubles.
 __device__ __forceinline__ double block_sum(double v, double *red, int nw) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   v = warp_sum(v);
   if (lane == 0) red[warp] = v;
   __syncthreads();
-  double t = 0.0;
-  for (int w = 0; w < nw; w++) t += red[w];
-  return t;
+  if (warp == 0) {
+    double t = lane < nw ? red[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) red[kMaxWarps] = t;
+  }
+  __syncthreads();
+  return red[kMaxWarps];
 }
 
 // Real solid harmonics r^l Y_lm with the reference's constants (src/lsdft_tools.cc:165-187);
