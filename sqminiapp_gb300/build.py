@@ -13,6 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libsq_gb300.so")
+DRIVER = os.path.join(LIB_DIR, "sq_lsdft")  # the command-line program (csrc/driver.cpp)
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_LIB = "/usr/local/cuda/lib64"
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", CSRC,
@@ -77,6 +78,14 @@ def build(verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    src = os.path.join(CSRC, "driver.cpp")
+    if (not os.path.exists(DRIVER) or os.path.getmtime(DRIVER) < os.path.getmtime(LIB) or
+            os.path.getmtime(DRIVER) < os.path.getmtime(src)):
+        cmd = ["g++", "-O2", "-std=c++17", "-I", os.path.join(os.path.dirname(HERE), "include"),
+               src, "-o", DRIVER, "-L", LIB_DIR, "-lsq_gb300", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("driver build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     return LIB
 
 
