@@ -68,6 +68,11 @@ def check_layout(n, precision, flags):
         # the second point of the last pair of an odd-width row is a pad slot (never written)
         if n % 2:
             assert owner[off + (n - 1) + 1] == -1
+        # U pairs: the pair (px, px+1) of row y, plane z stays inside its own row of upitch
+        nc = upitch * n * n
+        for zz, yy in ((0, 0), (n - 1, n - 1)):
+            first = (zz * n + yy) * upitch + px
+            assert np.all(first + 1 < (zz * n + yy + 1) * upitch) and (first + 1).max() < nc
     return psize
 
 
