@@ -196,9 +196,11 @@ sq_status sq_measure_fp32_peak(int device, double *tflops);
  * on a static scratch array of the library (about 410 KiB per GPU, held until exit).
  * DEVICE inputs d_lambda, d_weights [n_nodes][n_qp]; d_rho [n_nodes] may be NULL; the
  * HOST array out[3] receives lambda_f, e_band and ts; maxit <= 200 (else SQ_CAPACITY).
- * The first call on a device looks up the array's address, so make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race.  Synchronises
- * `stream` before returning. */
+ * Every call looks the array's address up in the current context (no allocation).  Calls
+ * share the array: calls that overlap on the GPU race.  Synchronises `stream` before
+ * returning, so it cannot be called while `stream` is being captured (SQ_BAD_INPUT).
+ * SQ_NO_CONVERGENCE (out[] still filled with the last midpoint) when the bisection used all
+ * maxit steps without narrowing the bracket below tol. */
 sq_status sq_fermi_density_energy_noalloc(const double *d_lambda, const double *d_weights,
                                           long n_nodes, int n_qp, double beta,
                                           double n_electrons, double dV, double tol, int maxit,

@@ -6,6 +6,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = os.path.join(HERE, "lib", "libsq_gb300.so")
 
 SQ_OK = 0
+SQ_BAD_INPUT = 1
+SQ_NO_CONVERGENCE = 2
+SQ_LANCZOS_BREAKDOWN = 3
+SQ_DEVICE_TIMEOUT = 4
+SQ_CUDA_ERROR = 5
+SQ_CAPACITY = 6
 STATUS_NAMES = {0: "SQ_OK", 1: "SQ_BAD_INPUT", 2: "SQ_NO_CONVERGENCE", 3: "SQ_LANCZOS_BREAKDOWN",
                 4: "SQ_DEVICE_TIMEOUT", 5: "SQ_CUDA_ERROR", 6: "SQ_CAPACITY"}
 

@@ -16,7 +16,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 #include <string>
 
 #include "sq_gb300.h"
@@ -276,6 +275,11 @@ cudaError_t launch_fermi(const double *lambda, const double *w, long long n_node
 // everything else is written before it is read.  Two calls whose work overlaps on the GPU
 // (on different streams, or from different host threads) race on the array and give wrong
 // results; calls must be ordered.
+//
+// The array's device address belongs to the CUDA context that is current when it is looked
+// up, so every call looks it up again with cudaGetSymbolAddress (no allocation): a context
+// that was destroyed and made again, or another context made current by the caller, never
+// sees a stale address.
 // ---------------------------------------------------------------------------------------
 namespace {
 constexpr int kNoallocMaxBlocks = 256;
@@ -291,10 +295,6 @@ struct NoallocScratch {
 };
 
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
-
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-NoallocScratch *g_noalloc_ptr[kMaxDevices] = {};
 }  // namespace
 
 extern "C" sq_status sq_fermi_density_energy_noalloc(const double *d_lambda,
@@ -315,27 +315,32 @@ extern "C" sq_status sq_fermi_density_energy_noalloc(const double *d_lambda,
                       " (capacity of the static scratch array)");
     return SQ_CAPACITY;
   }
+  cudaStream_t s = (cudaStream_t)stream;
+  // the call ends with a device-to-host copy and a stream synchronisation, neither of which a
+  // stream capture allows: refuse before touching the stream
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cap);
+  if (e != cudaSuccess) {
+    set_noalloc_error(std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(e));
+    return SQ_CUDA_ERROR;
+  }
+  if (cap != cudaStreamCaptureStatusNone) {
+    set_noalloc_error("the stream is being captured; this call synchronises it and cannot be "
+                      "captured");
+    return SQ_BAD_INPUT;
+  }
   int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) {
     set_noalloc_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     return SQ_CUDA_ERROR;
   }
-  // set-up, once per device, with that device current: resolve the array's device address
-  NoallocScratch *scr = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-      void *ptr = nullptr;
-      e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-      if (e != cudaSuccess) {
-        set_noalloc_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        return SQ_CUDA_ERROR;
-      }
-      g_noalloc_ptr[dev] = reinterpret_cast<NoallocScratch *>(ptr);
-    }
-    scr = g_noalloc_ptr[dev];
+  // the array's address in the current context (looked up on every call, see above)
+  void *ptr = nullptr;
+  if ((e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch)) != cudaSuccess) {
+    set_noalloc_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    return SQ_CUDA_ERROR;
   }
+  NoallocScratch *scr = reinterpret_cast<NoallocScratch *>(ptr);
   int sms = 0, per_sm = 0;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
       (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fermi_kernel, kFermiBlock, 0)) !=
@@ -349,7 +354,6 @@ extern "C" sq_status sq_fermi_density_energy_noalloc(const double *d_lambda,
   }
   // one CTA per SM (co-resident for the cooperative launch), as the handle-based path uses
   const int grid = std::min(sms, kNoallocMaxBlocks);
-  cudaStream_t s = (cudaStream_t)stream;
   if ((e = cudaMemsetAsync(&scr->status, 0, sizeof(int), s)) != cudaSuccess ||
       (e = launch_fermi(d_lambda, d_weights, n_nodes, n_qp, beta, n_electrons, dV, tol, maxit,
                         d_rho, scr->out, scr->partials, scr->barrier, &scr->status, grid, s)) !=
@@ -373,6 +377,13 @@ extern "C" sq_status sq_fermi_density_energy_noalloc(const double *d_lambda,
   out[0] = res[0];
   out[1] = res[1];
   out[2] = res[2];
+  // res[3] = bisection steps taken; the kernel leaves the loop early once hi - lo < tol, so
+  // reaching maxit means the bracket never got that narrow
+  if (res[3] >= (double)maxit) {
+    set_noalloc_error("Fermi bisection did not reach tol in maxit steps (outputs hold the last "
+                      "midpoint)");
+    return SQ_NO_CONVERGENCE;
+  }
   return SQ_OK;
 }
 

@@ -76,25 +76,31 @@ def check_layout(n, precision, flags):
     return psize
 
 
-def _cube_sizes():
-    # (rcut, h) -> cube 2*ceil(rcut/h)+1 from 9 to 33 on a 4-atom cell
-    return [(4.0, 0.5), (6.0, 0.5), (6.5, 0.5), (7.0, 0.5), (7.5, 0.5), (7.0, 8.5 / 19),
-            (3.4, 0.85), (5.0, 0.5)]
+# (rcut, h, precision) -> cube 2*ceil(rcut/h)+1 from 9 to 33 on a 4-atom cell, and whether
+# the planner must accept it.  FP64 cubes of 31^3 and up fit no single-CTA layout.
+_CASES = [(4.0, 0.5, 32, True), (4.0, 0.5, 64, True), (6.0, 0.5, 32, True), (6.0, 0.5, 64, True),
+          (6.5, 0.5, 32, True), (6.5, 0.5, 64, True), (7.0, 0.5, 32, True), (7.0, 0.5, 64, True),
+          (7.5, 0.5, 32, True), (7.5, 0.5, 64, False), (7.0, 8.5 / 19, 32, True),
+          (7.0, 8.5 / 19, 64, False), (3.4, 0.85, 32, True), (3.4, 0.85, 64, True),
+          (5.0, 0.5, 32, True), (5.0, 0.5, 64, True)]
 
 
-@pytest.mark.parametrize("rcut,h", _cube_sizes())
-@pytest.mark.parametrize("precision", [32, 64])
-def test_kernel_index_arithmetic_stays_in_bounds(rcut, h, precision, tmp_path):
+@pytest.mark.parametrize("rcut,h,precision,fits", _CASES)
+def test_kernel_index_arithmetic_stays_in_bounds(rcut, h, precision, fits, tmp_path):
     d, name, _ = make_fcc_mg_deck(str(tmp_path), "c", ncell=1, h=h, rcut=rcut, n_qp=20)
-    try:
-        p = plan_kernel(d, name, precision=precision)
-    except Exception as e:  # a cube that fits no layout at this precision is refused
-        assert "does not fit" in str(e) or "FP32" in str(e)
+    if not fits:
+        with pytest.raises(Exception) as e:
+            plan_kernel(d, name, precision=precision)
+        assert "does not fit" in str(e.value) or "FP32" in str(e.value)
         return
+    p = plan_kernel(d, name, precision=precision)
     n = p.cube[0]
+    assert n == 2 * int(np.ceil(rcut / h - 1e-12)) + 1
     flags = p.kernel_layout & 7
     if n > 32:
         assert precision == 32 and flags & WIDE
     psize = check_layout(n, precision, flags)
+    # the kernel rounds P up to whole 16-byte vectors before U and the lists
+    psize_kernel = (psize + 3) & ~3
     elem = 4 if precision == 32 else 8
-    assert elem * psize < p.kernel_smem_bytes
+    assert elem * psize_kernel < p.kernel_smem_bytes

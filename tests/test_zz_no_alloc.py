@@ -65,3 +65,24 @@ def test_noalloc_rejects_oversize(deck_dir):
         1e-12, 201, None, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None)
     assert st != SQ_OK
     assert "maxit" in L.sq_last_error_string().decode()
+
+
+def test_noalloc_reports_unconverged_bisection(deck_dir):
+    """One bisection step cannot narrow a bracket of several Ha to 1e-12: the call says so
+    (SQ_NO_CONVERGENCE) instead of returning the midpoint as converged."""
+    import torch
+    from sqminiapp_gb300.capi import SQ_NO_CONVERGENCE, SQ_OK, lib
+
+    dev = torch.device("cuda", 0)
+    lam = torch.tensor([[-1.0, 0.5], [0.2, 2.0]], dtype=torch.float64, device=dev)
+    w = torch.full((2, 2), 0.5, dtype=torch.float64, device=dev)
+    out = np.zeros(3)
+    L = lib()
+    dp = ctypes.POINTER(ctypes.c_double)
+    args = (ctypes.c_void_p(lam.data_ptr()), ctypes.c_void_p(w.data_ptr()), 2, 2, 30.0, 2.0,
+            1.0, 1e-12)
+    st = L.sq_fermi_density_energy_noalloc(*args, 1, None, out.ctypes.data_as(dp), None)
+    assert st == SQ_NO_CONVERGENCE, L.sq_last_error_string().decode()
+    assert np.isfinite(out[0])
+    st = L.sq_fermi_density_energy_noalloc(*args, 200, None, out.ctypes.data_as(dp), None)
+    assert st == SQ_OK, L.sq_last_error_string().decode()
