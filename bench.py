@@ -67,6 +67,10 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--max-nodes", type=int, default=0,
                    help="process only the first N nodes per step (profiling of small cases)")
+    p.add_argument("--kernel", type=int, choices=[0, 1, 2], default=0,
+                   help="FP32 Lanczos kernel: 0 automatic, 1 single-pass, 2 split-pass")
+    p.add_argument("--tile", type=int, default=0,
+                   help="split-pass kernel tile (z-/y-ranges per row); 0 autotuned")
     p.add_argument("--list-format", type=int, choices=[0, 1, 2], default=0,
                    help="projector-list records of the main workload: 0 automatic, 1 full, "
                         "2 compact")
@@ -247,7 +251,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     (deck_dir, name, meta), cfg = make_deck(args.config, rank)
     eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local,
-                list_format=args.list_format)
+                list_format=args.list_format, kernel=args.kernel, tile=args.tile)
     n, q = eng.n_nodes, eng.n_qp
     if args.max_nodes > 0:
         n = min(n, args.max_nodes)
@@ -318,7 +322,9 @@ def run_ours(args):
     tp = os.path.join(ROOT, "profiles", "lanczos_traffic.txt")
     if os.path.exists(tp):
         kv = dict(line.split(":", 1) for line in open(tp) if ":" in line and not line.startswith("#"))
-        if kv.get("workload", "").strip() == args.config and args.max_nodes == 0:
+        same_kernel = kv.get("kernel", "lanczos_kernel<float>").strip() == (
+            "lanczos_quad_kernel" if eng.info.kernel_layout & 16 else "lanczos_kernel<float>")
+        if kv.get("workload", "").strip() == args.config and args.max_nodes == 0 and same_kernel:
             traffic = float(kv["bytes_per_launch"])
 
     # e2e through the host-buffer API
@@ -392,7 +398,9 @@ def run_ours(args):
                                          "smem_bytes": eng.info.kernel_smem_bytes}},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": float(peak[0]),
                          "unit": "TFLOP/s", "frac": achieved / float(peak[0]),
-                         "traffic": traffic, "kernel": "lanczos_kernel<float>",
+                         "traffic": traffic,
+                         "kernel": ("lanczos_quad_kernel" if eng.info.kernel_layout & 16
+                                    else "lanczos_kernel<float>"),
                          "kernel_ms": lz_ms, "flops_per_launch": flops,
                          "peak_kind": "measured FP32 FMA probe",
                          "peak_theoretical": peak_theory,

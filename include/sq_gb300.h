@@ -53,6 +53,14 @@ typedef struct sq_options {
    * point), 2 compact (T_l per channel and box coordinates; chi_lm rebuilt while streaming).
    * FP64 and the faithful operator always use the full format. */
   int list_format;
+  /* FP32 Lanczos kernel: 0 automatic (the split-pass kernel where it applies: corrected
+   * operator, cubes at most 32 points wide, both vectors and the full lists fit), 1 the
+   * single-pass kernel, 2 the split-pass kernel (SQ_BAD_INPUT where it does not apply). */
+  int kernel;
+  /* Split-pass kernel tile: z-ranges per cube row in the z pass and y-ranges per plane in the
+   * y pass (threads = ceil(nx/4) * max(ny,nz) * tile); 0 automatic (the engine's autotuner
+   * times the candidates on the first call and keeps the fastest). */
+  int tile;
 } sq_options;
 
 /* Engine facts after setup. */
@@ -80,8 +88,9 @@ typedef struct sq_info {
   double proj_points_per_node;  /* mean over nodes of sum_images |projector box ∩ cube| */
   /* Lanczos kernel configuration (0 from sq_describe_deck): vector layout flags (1 = zero rows
    * between z-planes, FP32; 2 = cubes wider than 32 points, FP32; 4 = rows without zero
-   * columns, FP64; 8 = compact projector list), U on chip (1) or in global scratch (0),
-   * threads per CTA, shared memory bytes per CTA. */
+   * columns, FP64; 8 = compact projector list; 16 = split-pass kernel over 16-byte quads,
+   * FP32), U on chip (1) or in global scratch (0), threads per CTA, shared memory bytes per
+   * CTA. */
   int kernel_layout;
   int kernel_u_on_chip;
   int kernel_threads;

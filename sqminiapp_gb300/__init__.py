@@ -51,13 +51,17 @@ class LSDFT:
     corrected operator.  precision=32 runs FP32 Lanczos vectors with FP64 recurrence
     coefficients, quadrature and sums; precision=64 is FP64 throughout.  list_format picks
     the FP32 corrected operator's projector-list records (0 automatic, 1 full chi_lm, 2
-    compact radial values; sq_options.list_format).
+    compact radial values; sq_options.list_format); kernel the FP32 Lanczos kernel (0
+    automatic, 1 single-pass, 2 split-pass) and tile the split-pass kernel's z-/y-ranges per
+    row (0: timed on the first call).
     """
 
-    def __init__(self, deck_dir, name, faithful=False, precision=32, device=0, list_format=0):
+    def __init__(self, deck_dir, name, faithful=False, precision=32, device=0, list_format=0,
+                 kernel=0, tile=0):
         self._lib = lib()
         self._h = ctypes.c_void_p()
-        opt = SqOptions(int(bool(faithful)), int(precision), int(device), int(list_format))
+        opt = SqOptions(int(bool(faithful)), int(precision), int(device), int(list_format),
+                        int(kernel), int(tile))
         check(self._lib.sq_create_from_deck(deck_dir.encode(), name.encode(), ctypes.byref(opt),
                                             ctypes.byref(self._h)), "sq_create_from_deck")
         info = SqInfo()
@@ -312,12 +316,14 @@ class LSDFT:
                 "e_self": sc[0], "e_self_ref": sc[1], "e_corr": sc[2], "b_total": sc[3]}
 
 
-def plan_kernel(deck_dir, name, faithful=False, precision=32, list_format=0, device=None):
+def plan_kernel(deck_dir, name, faithful=False, precision=32, list_format=0, device=None,
+                kernel=0, tile=0):
     """Host-only plan (sq_plan_kernel): the SqInfo an engine for this deck would report on a
     device with the given properties (default GB300_DEVICE), kernel_* fields included."""
     dev = dict(GB300_DEVICE, **(device or {}))
     info = SqInfo()
-    opt = SqOptions(int(bool(faithful)), int(precision), 0, int(list_format))
+    opt = SqOptions(int(bool(faithful)), int(precision), 0, int(list_format), int(kernel),
+                    int(tile))
     check(lib().sq_plan_kernel(deck_dir.encode(), name.encode(), ctypes.byref(opt),
                                int(dev["num_sms"]), int(dev["smem_optin"]), int(dev["l2_bytes"]),
                                ctypes.byref(info)), "sq_plan_kernel")

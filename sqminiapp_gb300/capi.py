@@ -26,7 +26,7 @@ _fp = ctypes.POINTER(ctypes.c_float)
 
 class SqOptions(ctypes.Structure):
     _fields_ = [("faithful", ctypes.c_int), ("precision", ctypes.c_int), ("device", ctypes.c_int),
-                ("list_format", ctypes.c_int)]
+                ("list_format", ctypes.c_int), ("kernel", ctypes.c_int), ("tile", ctypes.c_int)]
 
 
 class SqInfo(ctypes.Structure):

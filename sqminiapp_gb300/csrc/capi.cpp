@@ -306,7 +306,38 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
   const bool faithful = h->opt.faithful != 0;
   h->u_smem = false;
   p.layout = 0;
-  if (h->opt.precision == 32) {
+  p.zchunks = 1;
+  p.vq_row = 4 * ((p.EX + 6 + 3) / 4);  // the row of a quad-aligned Veff copy (see below)
+  p.vq_copy_stride = (long long)p.vq_row * p.EY * p.EZ;
+  h->quad = false;
+  if (h->opt.kernel < 0 || h->opt.kernel > 2 || h->opt.tile < 0)
+    throw std::invalid_argument("sq_options.kernel must be 0, 1 or 2 and tile >= 0");
+  if (h->opt.precision == 32 && !faithful && !wide && h->opt.kernel != 1 &&
+      h->opt.list_format != 2) {
+    // split-pass kernel over 16-byte quads: P and U on chip as [nz][ny][4 ceil(nx/4)], full
+    // projector records, which must stay in L2 together (152 CTAs' lists)
+    sq::LanczosParams q = p;
+    q.layout = sq::kLayoutQuad;
+    q.pitch = q.upitch = 4 * ((p.nx + 3) / 4);
+    q.zchunks = h->opt.tile > 0 ? h->opt.tile : 2;
+    const int threads = sq::lanczos_quad_threads(q);
+    const double list_bytes = (double)h->num_sms * projector_points_per_node(s, d) *
+                              kept_fraction(s) *
+                              (double)sq::proj_record_bytes(4, false, p.union_mask, false);
+    if (threads <= sq::kQuadMaxThreads && sq::lanczos_quad_smem_bytes(q) <= (size_t)smem_optin &&
+        (h->opt.list_format == 1 || list_bytes <= 0.75 * (double)l2_bytes)) {
+      p = q;
+      h->quad = true;
+      h->u_smem = true;
+      h->block = threads;
+    }
+  }
+  if (h->opt.kernel == 2 && !h->quad)
+    throw std::invalid_argument("the split-pass FP32 kernel does not apply to this cell and options "
+                                "(FP32, corrected operator, cubes at most 32 wide, lists in L2)");
+  if (h->quad) {
+    // nothing else to choose: layout, threads and lists are fixed above
+  } else if (h->opt.precision == 32) {
     // first choice: y gaps and U on chip; then U on chip without the gaps (y bounds-checked);
     // then y gaps with U in global scratch
     const size_t optin = (size_t)smem_optin;
@@ -321,7 +352,7 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
       }
     }
   }
-  if (h->opt.precision == 32 && !faithful && h->opt.list_format != 1) {
+  if (!h->quad && h->opt.precision == 32 && !faithful && h->opt.list_format != 1) {
     // compact records when the full lists of all SMs (plus U slices in global scratch) would
     // take more than 3/4 of the L2, or on request; only if the extra per-image data fits
     bool compact = h->opt.list_format == 2;
@@ -338,7 +369,8 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
       if (sq::lanczos_smem_bytes(q, 4, h->u_smem, faithful) <= (size_t)smem_optin) p = q;
     }
   }
-  h->smem = sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
+  h->smem = h->quad ? sq::lanczos_quad_smem_bytes(p)
+                    : sq::lanczos_smem_bytes(p, (int)h->elem, h->u_smem, faithful);
   if (h->smem > (size_t)smem_optin && h->opt.precision == 64) {
     p.pitch = p.nx;  // rows without zero columns; the kernel bounds-checks x instead
     p.layout = sq::kLayoutXClamp;
@@ -349,7 +381,7 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
                                 "x" + std::to_string(p.nz) +
                                 " does not fit in shared memory at this precision");
   h->grid = h->num_sms;
-  {  // projector records pack the P and U indices of a cube point into 16 bits each
+  if (!h->quad) {  // projector records pack the P and U indices of a cube point into 16 bits each
     const long long pitch_rows = (p.layout & sq::kLayoutYGap) ? p.ny + sq::kStencilHalf : p.ny;
     const long long psize = (long long)sq::kStencilHalf * p.pitch + (long long)p.nz * pitch_rows * p.pitch;
     if (psize >= 65536 || (long long)p.upitch * p.ny * p.nz >= 65536)
@@ -394,7 +426,9 @@ void build_engine(sq_handle *h) {
     ck(cudaMemcpy(h->d_tables, s.tables.data(), 8 * s.tables.size(), cudaMemcpyHostToDevice),
        "tables H2D");
   }
-  dev_alloc(&h->d_veff_ext, h->elem * (size_t)p.EX * p.EY * p.EZ, "veff_ext");
+  dev_alloc(&h->d_veff_ext,
+            h->quad ? sizeof(float) * sq::veff_quad_floats(p) : h->elem * (size_t)p.EX * p.EY * p.EZ,
+            "veff_ext");
   dev_alloc(&h->d_veff_in, sizeof(double) * (size_t)p.Nx * p.Ny * p.Nz, "veff");
   if (!h->u_smem) {
     const size_t nc4 = ((size_t)p.upitch * p.ny * p.nz + 3) & ~size_t(3);
@@ -468,6 +502,42 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   ck(cudaStreamIsCapturing(s, &cap), "capture status");
   const bool timed = cap == cudaStreamCaptureStatusNone;  // no timing events inside a graph
+  if (h->quad && !h->tuned && h->opt.tile == 0 && timed && n >= 2LL * grid) {
+    // autotune the split-pass kernel's tile (z- / y-ranges per row / plane) on this call's
+    // first nodes, one node per CTA per candidate, and keep the fastest for the handle
+    cudaEvent_t t0, t1;
+    ck(cudaEventCreate(&t0), "event");
+    ck(cudaEventCreate(&t1), "event");
+    float best = 1e30f;
+    int best_tile = p.zchunks;
+    for (int tile = 1; tile <= 4; tile++) {
+      sq::LanczosParams q = p;
+      q.zchunks = tile;
+      q.node_end = nb + grid;
+      const int threads = sq::lanczos_quad_threads(q);
+      if (threads > sq::kQuadMaxThreads) break;
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; rep++) {  // the first launch of a tile loads its code
+        ck(cudaEventRecord(t0, s), "event");
+        ck(sq::launch_lanczos(q, 32, false, true, grid, threads, h->smem, s, h->d_veff_ext,
+                              h->d_images, h->d_tables, h->d_u, h->d_proj, h->d_ab, h->d_status),
+           "lanczos (tile probe)");
+        ck(cudaEventRecord(t1, s), "event");
+        ck(cudaEventSynchronize(t1), "event");
+        ck(cudaEventElapsedTime(&ms, t0, t1), "event");
+      }
+      if (ms < best) {
+        best = ms;
+        best_tile = tile;
+      }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    h->lp.zchunks = p.zchunks = best_tile;
+    h->block = sq::lanczos_quad_threads(p);
+    h->info.kernel_threads = h->block;
+    h->tuned = true;
+  }
   if (timed) {
     update_node_cost(h);
     h->cost_grid = grid;

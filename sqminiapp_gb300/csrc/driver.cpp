@@ -39,7 +39,7 @@ int fail(const char *what) {
 
 int main(int argc, char **argv) {
   std::string name, dir = ".", lambdas, den, out;
-  sq_options opt = {0, 32, 0, 0};
+  sq_options opt = {0, 32, 0, 0, 0, 0};
   bool scf = false;
   for (int i = 1; i < argc; i++) {
     const std::string a = argv[i];

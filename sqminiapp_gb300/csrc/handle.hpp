@@ -69,6 +69,8 @@ struct sq_handle {
   sq::LanczosParams lp{};
   int num_sms = 0;
   bool u_smem = false;
+  bool quad = false;    // the split-pass FP32 kernel (kLayoutQuad)
+  bool tuned = false;   // its tile has been chosen (sq_options.tile, or timed on a first call)
   size_t smem = 0;
   int grid = 0;
   int block = 0;

@@ -26,6 +26,33 @@ __global__ void veff_extend_kernel(const double *__restrict__ veff, double vcons
   }
 }
 
+// Quad-aligned copies of cdiag + Veff for the split-pass kernel: copy c holds extended x index
+// ex at row position ex + c, so a node at grid x = I reads its cube row from copy (4 - I%4)%4
+// at a 16-byte boundary; positions outside [c, c + EX) hold 0.
+__global__ void veff_quad_kernel(const double *__restrict__ veff, double vconst, double cdiag,
+                                 float *__restrict__ out, int Nx, int Ny, int Nz, int nhx, int nhy,
+                                 int nhz, int EX, int EY, int EZ, int row) {
+  const long long per_copy = (long long)row * EY * EZ;
+  const long long total = 4 * per_copy;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / per_copy);
+    const long long r = e - c * per_copy;
+    const int pos = (int)(r % row);
+    const long long rr = r / row;
+    const int ey = (int)(rr % EY), ez = (int)(rr / EY);
+    const int ex = pos - c;
+    float v = 0.f;
+    if (ex >= 0 && ex < EX) {
+      const int gx = ((ex - nhx) % Nx + Nx) % Nx;
+      const int gy = ((ey - nhy) % Ny + Ny) % Ny;
+      const int gz = ((ez - nhz) % Nz + Nz) % Nz;
+      v = float(cdiag + (veff ? veff[((long long)gz * Ny + gy) * Nx + gx] : vconst));
+    }
+    out[e] = v;
+  }
+}
+
 }  // namespace
 
 int kernel_mask(int union_mask) {
@@ -92,6 +119,11 @@ cudaError_t launch_lanczos_f32_wide(int mask, bool faithful, const LanczosParams
                                     const ImageMeta *images, const void *tables, void *u_scratch,
                                     void *proj_scratch, double *ab, int *status);
 
+cudaError_t launch_lanczos_f32_quad(int mask, const LanczosParams &p, int grid, int block,
+                                    size_t smem, cudaStream_t s, const void *veffq,
+                                    const ImageMeta *images, const void *tables,
+                                    void *proj_scratch, double *ab, int *status);
+
 cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful, bool u_smem,
                            int grid, int block, size_t smem, cudaStream_t s, const void *veff_ext,
                            const ImageMeta *images, const void *tables, void *u_scratch,
@@ -99,6 +131,11 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
   const int mask = kernel_mask(p.union_mask);
   const bool gap = (p.layout & kLayoutYGap) != 0;
   if (precision == 32) {
+    if (p.layout & kLayoutQuad) {  // corrected operator, full records, P and U on chip
+      if (faithful || !u_smem || (p.layout & ~kLayoutQuad)) return cudaErrorInvalidValue;
+      return launch_lanczos_f32_quad(mask, p, grid, block, smem, s, veff_ext, images, tables,
+                                     proj_scratch, ab, status);
+    }
     if (p.layout & kLayoutCompact) {  // corrected operator only
       if (faithful) return cudaErrorInvalidValue;
       return launch_lanczos_f32_compact(mask, u_smem, p, grid, block, smem, s, veff_ext, images,
@@ -124,6 +161,14 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
 
 cudaError_t launch_veff_extend(const double *veff, double vconst, void *ext, int precision,
                                const LanczosParams &p, cudaStream_t s) {
+  if (p.layout & kLayoutQuad) {
+    const long long total = (long long)veff_quad_floats(p);
+    const int block = 256;
+    const int grid = (int)std::min<long long>((total + block - 1) / block, 152LL * 16);
+    veff_quad_kernel<<<grid, block, 0, s>>>(veff, vconst, p.cdiag, (float *)ext, p.Nx, p.Ny, p.Nz,
+                                            p.nhx, p.nhy, p.nhz, p.EX, p.EY, p.EZ, p.vq_row);
+    return cudaGetLastError();
+  }
   const long long total = (long long)p.EX * p.EY * p.EZ;
   const int block = 256;
   const int grid = (int)std::min<long long>((total + block - 1) / block, 152LL * 16);

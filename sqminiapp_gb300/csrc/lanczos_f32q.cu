@@ -1,0 +1,56 @@
+// lanczos_f32q.cu -- instantiations of the split-pass FP32 Lanczos kernel (kLayoutQuad) and its
+// host-side sizes.
+#include "lanczos_quad.cuh"
+
+namespace sq {
+
+int lanczos_quad_threads(const LanczosParams &p) {
+  // pitch/4 threads per row (pass A) or plane (pass B), zchunks ranges each
+  const int groups = std::max(p.ny, p.nz) * p.zchunks;
+  return 32 * (((p.pitch / 4) * groups + 31) / 32);
+}
+
+size_t lanczos_quad_smem_bytes(const LanczosParams &p) {
+  const size_t nc = (size_t)p.nz * p.ny * p.pitch;
+  const int nlm = mask_nlm(kernel_mask(p.union_mask));
+  size_t b = sizeof(float) * 2 * nc;                          // P, U
+  b += sizeof(double) * (2 * lk::kMaxWarps + 128);           // a_k / b_k partials, a[], b[]
+  b += sizeof(float) * 2 * (size_t)p.max_img * nlm;           // gathered c, alpha
+  b += sizeof(int) * (8 * (size_t)p.max_img + 2) + sizeof(int) * 4;  // per-node image lists
+  return b;
+}
+
+size_t veff_quad_floats(const LanczosParams &p) { return 4 * (size_t)p.vq_copy_stride; }
+
+namespace {
+template <int MAXT, bool ISO>
+cudaError_t launch_quad_mask(int mask, const LanczosParams &p, int grid, int block, size_t smem,
+                             cudaStream_t s, const void *veffq, const ImageMeta *images,
+                             const void *tables, void *proj_scratch, double *ab, int *status) {
+  switch (mask) {
+    case 3: return lq::launch_quad_variant<3, MAXT, ISO>(p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+    case 5: return lq::launch_quad_variant<5, MAXT, ISO>(p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+    case 6: return lq::launch_quad_variant<6, MAXT, ISO>(p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+    case 7: return lq::launch_quad_variant<7, MAXT, ISO>(p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+    default: return lq::launch_quad_variant<15, MAXT, ISO>(p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+  }
+}
+}  // namespace
+
+// Two register budgets: up to 12 warps (3 per SM sub-partition: 168 registers a thread) and up
+// to 16 warps (128).  Isotropic meshes (hx = hy = hz) share one set of stencil weights.
+cudaError_t launch_lanczos_f32_quad(int mask, const LanczosParams &p, int grid, int block,
+                                    size_t smem, cudaStream_t s, const void *veffq,
+                                    const ImageMeta *images, const void *tables,
+                                    void *proj_scratch, double *ab, int *status) {
+  bool iso = true;
+  for (int d = 0; d <= kStencilHalf; d++)
+    iso = iso && p.cxf[d] == p.czf[d] && p.cyf[d] == p.czf[d];
+  if (block <= 384)
+    return iso ? launch_quad_mask<384, true>(mask, p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status)
+               : launch_quad_mask<384, false>(mask, p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+  return iso ? launch_quad_mask<kQuadMaxThreads, true>(mask, p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status)
+             : launch_quad_mask<kQuadMaxThreads, false>(mask, p, grid, block, smem, s, veffq, images, tables, proj_scratch, ab, status);
+}
+
+}  // namespace sq

@@ -1,0 +1,584 @@
+// lanczos_quad.cuh -- FP32 Lanczos kernel with split stencil passes over aligned quads.
+//
+// Same recurrence and operator as lanczos_kernel.cuh (src/lsdft_scf.cc:119-147 with
+// H = -1/2 Lap (12th-order FD, Dirichlet cube, src/lsdft_initObjs.cc:393-475) + diag(Veff)
+// + the Kleinman-Bylander projectors of the atom images that meet the cube,
+// src/lsdft_matvec.cc:25-149); FP32 vectors, corrected operator, full projector records.
+//
+// Layout.  P and U are both [nz][ny][pitch] floats in shared memory, pitch = 4*ceil(nx/4):
+// every row starts on a 16-byte boundary and holds whole float4 quads; the pad columns
+// [nx, pitch) stay zero.  There are no zero rows or columns between rows: neighbours outside
+// the cube are never loaded (x: the quad loads are predicated off at the row ends; y and z:
+// the register rings start and end with zeros).  A point's P and U indices are the same,
+// (z*ny + y)*pitch + x.
+//
+// Stencil, split by axis so that two of the three axes come from registers:
+//   pass A  a thread owns one quad (x..x+3) of row y over a z-range and walks z with a
+//           13-plane register ring (one float4 load per plane); the x neighbours of the quad
+//           are four aligned float4 loads of the same row; it adds the diagonal (cdiag + Veff,
+//           read as one aligned float4 from a quad-aligned copy of the padded potential) and
+//           forms U <- (diag + Dz + Dx) v - b U;
+//   pass B  a thread owns one quad of plane z over a y-range and walks y with a 13-row
+//           register ring: U += Dy v.
+// Eight consecutive threads own the quads of one row (pass A) or one plane (pass B), so a
+// quarter-warp's float4 accesses cover one contiguous row: no bank conflicts.
+//
+// Per Lanczos step (P = b v_k unnormalised, U = v_{k-1}), four CTA barriers:
+//   1  projector gather c = chi^T P (per-warp ranges of the node's list)  ||  pass A
+//   2  pass B  ||  alpha = Gamma c / b (and <v, V_nl v>)  -> per-warp partials of a_k
+//   3  projector scatter U += chi alpha  ||  every warp reduces the a_k partials
+//   4  w = U - a_k v, P <- w, U <- v  -> per-warp partials of b_k^2
+// After barrier 4 every warp reduces the b partials itself (the same FP64 tree in every warp,
+// so every thread sees the same b_k and takes the same branch).  a_k and b_k^2 are summed per
+// thread in FP32 with Kahan compensation, then across threads in FP64.
+#pragma once
+
+#include "lanczos_kernel.cuh"
+
+namespace sq {
+namespace lq {
+
+using lk::O;
+using lk::W;
+using lk::kMaxWarps;
+
+// Blackwell packed FP32 (PTX .f32x2, sm_100+): two lanes of float2 per instruction.
+__device__ __forceinline__ unsigned long long as_u64(float2 a) {
+  return *reinterpret_cast<unsigned long long *>(&a);
+}
+__device__ __forceinline__ float2 as_f2(unsigned long long r) {
+  return *reinterpret_cast<float2 *>(&r);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {  // a*b + c
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(as_u64(a)), "l"(as_u64(b)), "l"(as_u64(c)));
+  return as_f2(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(as_u64(a)), "l"(as_u64(b)));
+  return as_f2(d);
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(as_u64(a)), "l"(as_u64(b)));
+  return as_f2(d);
+}
+__device__ __forceinline__ float2 lo(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 splat(float c) { return make_float2(c, c); }
+
+// Kahan-compensated FP32 running sum.
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+// Sum of the kMaxWarps-entry array of per-warp partials (nw of them), the same FP64 butterfly
+// in every lane of every warp, so every thread gets the bit-identical total.
+__device__ __forceinline__ double all_reduce(const double *red, int nw) {
+  const int lane = threadIdx.x & 31;
+  double v = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int MASK, int MAXT, bool ISO>
+__global__ void __launch_bounds__(MAXT, 1)
+    lanczos_quad_kernel(const __grid_constant__ LanczosParams p, const float *__restrict__ veffq,
+                        const ImageMeta *__restrict__ images, const float *__restrict__ tables,
+                        unsigned char *proj_scratch, double *__restrict__ ab_out,
+                        int *__restrict__ status) {
+  constexpr int NLM = lk::Lm<MASK>::nlm;
+  using Rec = lk::ProjRec<float, NLM>;
+  constexpr int kStream = lk::stream_batch<Rec::nvec * (int)sizeof(typename Rec::vec_t)>();
+  const int nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
+  const int nq = pitch >> 2;        // quads per row
+  const int PS = ny * pitch;        // plane stride (floats)
+  const int PS4 = ny * nq;          // plane stride (quads)
+  const int nc = nz * PS;           // floats of P (and of U)
+  const int maxi = p.max_img;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *P = reinterpret_cast<float *>(smem_raw);
+  float *U = P + nc;
+  unsigned char *cur = reinterpret_cast<unsigned char *>(U + nc);
+  double *red_a = reinterpret_cast<double *>(cur);
+  double *red_b = red_a + kMaxWarps;
+  double *sab = red_b + kMaxWarps;  // a[64], b[64]
+  cur += sizeof(double) * (2 * kMaxWarps + 128);
+  float *cacc = reinterpret_cast<float *>(cur);
+  cur += sizeof(float) * maxi * NLM;
+  float *alpha = reinterpret_cast<float *>(cur);
+  cur += sizeof(float) * maxi * NLM;
+  int *img = reinterpret_cast<int *>(cur);
+  int *slot = img + maxi;
+  int *slot_type = slot + maxi;
+  int *blo = slot_type + maxi;
+  int *bext = blo + maxi;
+  int *pref = bext + maxi;      // maxi + 1
+  int *kept = pref + maxi + 1;
+  int *koff = kept + maxi;      // maxi + 1
+  int *cnt = koff + maxi + 1;   // [0] images, [1] slots, [2] overflow
+
+  typename Rec::vec_t *rec = reinterpret_cast<typename Rec::vec_t *>(
+      proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
+  unsigned *ridx = reinterpret_cast<unsigned *>(
+      reinterpret_cast<unsigned char *>(rec) + (size_t)p.proj_cap * sizeof(typename Rec::vec_t) * Rec::nvec);
+
+  const float4 *P4c = reinterpret_cast<const float4 *>(P);
+  float4 *P4 = reinterpret_cast<float4 *>(P);
+  float4 *U4 = reinterpret_cast<float4 *>(U);
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  // thread -> quad of a row (pass A) / of a plane (pass B): nq consecutive threads own the
+  // quads of one row or plane, so consecutive threads touch consecutive 16-byte quads
+  const int grp = threadIdx.x / nq, ql = threadIdx.x - grp * nq;
+  const int nch = p.zchunks;
+  const bool qin = true;
+  // pass A: row yA, z-range [zbA, zeA)
+  const int yA = grp % ny, zcA = grp / ny;
+  const int zlen = (nz + nch - 1) / nch;
+  const int zbA = min(nz, zcA * zlen), zeA = min(nz, zbA + zlen);
+  const bool actA = qin && zcA < nch && zbA < zeA;
+  // pass B: plane zB, y-range [ybB, yeB)
+  const int zB = grp % nz, ycB = grp / nz;
+  const int ylen = (ny + nch - 1) / nch;
+  const int ybB = min(ny, ycB * ylen), yeB = min(ny, ybB + ylen);
+  const bool actB = qin && ycB < nch && ybB < yeB;
+  // x neighbours of the quad inside the row; lanes of the last quad zero its pad points
+  const bool hm1 = ql >= 1, hm2 = ql >= 2, hp1 = ql + 1 < nq, hp2 = ql + 2 < nq;
+  const int x0 = 4 * ql;
+  const bool in1 = x0 + 1 < nx, in2 = x0 + 2 < nx, in3 = x0 + 3 < nx;  // x0 < nx always
+
+  for (long long node = p.node_begin + blockIdx.x; node < p.node_end; node += gridDim.x) {
+    const int I = (int)(node % p.Nx);
+    const int J = (int)((node / p.Nx) % p.Ny);
+    const int K = (int)(node / ((long long)p.Nx * p.Ny));
+    const int Xs = I - p.nhx, Ys = J - p.nhy, Zs = K - p.nhz;
+
+    // ---- per-node image list, slots and point offsets (warp 0); others clear ----
+    if (warp == 0) {
+      int count = 0;
+      for (int base = 0; base < p.n_images; base += 32) {
+        const int i = base + lane;
+        bool ok = false;
+        if (i < p.n_images) {
+          const int4 b = *reinterpret_cast<const int4 *>(&images[i]);
+          const TypeDesc &td = p.types[b.w];
+          ok = b.x <= Xs + nx - 1 && b.x + td.fx - 1 >= Xs && b.y <= Ys + ny - 1 &&
+               b.y + td.fy - 1 >= Ys && b.z <= Zs + nz - 1 && b.z + td.fz - 1 >= Zs;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        const int pos = count + __popc(m & ((1u << lane) - 1u));
+        if (ok && pos < maxi) img[pos] = i;
+        count += __popc(m);
+      }
+      __syncwarp();
+      const int n = min(count, maxi);
+      int slots = 0, offset = 0;
+      for (int base = 0; base < n; base += 32) {
+        const int k = base + lane;
+        bool start = false;
+        int npts = 0, lo = 0, ext = 0, atom = -1, type = 0;
+        if (k < n) {
+          const ImageMeta m = images[img[k]];
+          atom = m.atom;
+          type = m.type;
+          start = (k == 0) || images[img[k - 1]].atom != atom;
+          const TypeDesc &td = p.types[m.type];
+          const int xa = max(m.bx, Xs), ya = max(m.by, Ys), za = max(m.bz, Zs);
+          const int ex = min(m.bx + td.fx, Xs + nx) - xa;
+          const int ey = min(m.by + td.fy, Ys + ny) - ya;
+          const int ez = min(m.bz + td.fz, Zs + nz) - za;
+          npts = ex * ey * ez;
+          lo = (xa - Xs) | ((ya - Ys) << 10) | ((za - Zs) << 20);
+          ext = ex | (ey << 10) | (ez << 20);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, start);
+        const int g = slots + __popc(m & ((1u << lane) - 1u)) + (start ? 0 : -1);
+        int incl = npts;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (k < n) {
+          slot[k] = g;
+          if (start) slot_type[g] = type;
+          blo[k] = lo;
+          bext[k] = ext;
+          pref[k] = offset + incl - npts;
+        }
+        slots += __popc(m);
+        offset += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) {
+        pref[n] = offset;
+        cnt[0] = n;
+        cnt[1] = slots;
+        cnt[2] = count > maxi;
+      }
+    } else {
+      for (int e = threadIdx.x - 32; e < (nc >> 2); e += blockDim.x - 32) {
+        P4[e] = zero4;
+        U4[e] = zero4;
+      }
+      for (int e = threadIdx.x - 32; e < maxi * NLM; e += blockDim.x - 32) cacc[e] = 0.f;
+    }
+    __syncthreads();
+    const int n_img = cnt[0], n_slot = cnt[1];
+    if (cnt[2] || pref[n_img] > p.proj_cap) {  // capacity exceeded: report, NaN coefficients
+      if (threadIdx.x == 0) atomicOr(status, kStatusCapacity);
+      for (int j = threadIdx.x; j < 2 * p.nqp; j += blockDim.x)
+        ab_out[(node - p.node_begin) * 2 * p.nqp + j] = __longlong_as_double(0x7ff8000000000000ll);
+      __syncthreads();
+      continue;
+    }
+    if (threadIdx.x == 0) P[((nz - 1) / 2 * ny + (ny - 1) / 2) * pitch + (nx - 1) / 2] = 1.f;
+
+    // ---- this node's projector list: one warp per image, support points only ----
+    for (int kk = warp; kk < n_img; kk += nw) {
+      const lk::ImgView<float> v =
+          lk::load_view<float>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, 0, PS);
+      const int npts = pref[kk + 1] - pref[kk];
+      int kept_n = 0;
+      for (int q0 = 0; q0 < npts; q0 += 32) {
+        const int q = q0 + lane;
+        int lx, ly, lz;
+        lk::decode(v, min(q, npts - 1), lx, ly, lz);
+        const float dx = v.ox + p.hxf * float(lx), dy = v.oy + p.hyf * float(ly),
+                    dz = v.oz + p.hzf * float(lz);
+        const bool ok = q < npts && dx * dx + dy * dy + dz * dz <= v.r2max;
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+          const float *tb = v.tab + lz * v.fxy + ly * v.fx + lx;
+          float out[Rec::n];
+#pragma unroll
+          for (int s = 0; s < Rec::n; s++) out[s] = 0.f;
+          int chan = 0;
+          auto channel = [&](auto Lc) {
+            constexpr int L = decltype(Lc)::value;
+            if constexpr (MASK & (1 << L)) {
+              if (v.chan_mask & (1 << L)) {
+                const float t = tb[(chan++) * v.fvol];
+                lk::solid_harmonics<L, float>(dx, dy, dz, [&](int s, float ylm) {
+                  out[lk::Lm<MASK>::rank(s)] = ylm * t;
+                });
+              }
+            }
+          };
+          channel(std::integral_constant<int, 0>{});
+          channel(std::integral_constant<int, 1>{});
+          channel(std::integral_constant<int, 2>{});
+          channel(std::integral_constant<int, 3>{});
+          const int e = pref[kk] + kept_n + __popc(m & ((1u << lane) - 1u));
+          Rec::store(rec, e, out);
+          ridx[e] = (unsigned)(v.pbase + lz * PS + ly * pitch + lx);
+        }
+        kept_n += __popc(m);
+      }
+      if (lane == 0) kept[kk] = kept_n;
+    }
+    __syncthreads();
+    if (warp == 0) {  // exclusive scan of kept -> koff
+      int offset = 0;
+      for (int base = 0; base < n_img; base += 32) {
+        const int kk = base + lane;
+        const int c = kk < n_img ? kept[kk] : 0;
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (kk < n_img) koff[kk] = offset + incl - c;
+        offset += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0) koff[n_img] = offset;
+    }
+    __syncthreads();
+    const int total = koff[n_img];
+    const int per = (total + nw - 1) / nw;
+    const int r_begin = min(total, warp * per), r_end = min(total, r_begin + per);
+    int k_first = 0;  // image holding kept point r_begin: largest k with koff[k] <= r_begin
+    {
+      int lo = 0, hi = n_img;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (koff[mid] <= r_begin) lo = mid;
+        else hi = mid - 1;
+      }
+      k_first = min(lo, max(n_img - 1, 0));
+    }
+
+    // quad-aligned copy of the padded Veff + cdiag for this node (copy s: I + s = 0 mod 4)
+    const int sh = (4 - (I & 3)) & 3;
+    const float4 *vq = reinterpret_cast<const float4 *>(veffq + (size_t)sh * p.vq_copy_stride) +
+                       (size_t)((I + sh) >> 2);
+    const size_t VPS4 = (size_t)p.EY * (p.vq_row >> 2);  // plane stride in quads
+    const size_t VRS4 = (size_t)(p.vq_row >> 2);         // row stride in quads
+
+    double beta = 1.0;
+    for (int j = 0; j < p.nqp; j++) {
+      const float inv = float(1.0 / beta);
+      const float tb = float(beta);
+      const float2 inv2 = splat(inv), ntb2 = splat(-tb);
+
+      // ---- phase 1: projector gather  ||  pass A ----
+      {
+        int pos = r_begin, k = k_first;
+        while (pos < r_end) {
+          const int kend = min(r_end, koff[k + 1]);
+          const int shift = pref[k] - koff[k];
+          float acc[NLM];
+#pragma unroll
+          for (int s = 0; s < NLM; s++) acc[s] = 0.f;
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
+            float c[kStream][NLM];
+            unsigned ix[kStream];
+#pragma unroll
+            for (int u = 0; u < kStream; u++) {
+              const int e = min(i0 + 32 * u, kend - 1) + shift;
+              ix[u] = ridx[e];
+              Rec::load(rec, e, c[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kStream; u++) {
+              const float val = (i0 + 32 * u < kend) ? P[ix[u]] : 0.f;
+#pragma unroll
+              for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][s], val, acc[s]);
+            }
+          }
+          const int sl = slot[k];
+#pragma unroll
+          for (int s = 0; s < NLM; s++) {
+            const float r = lk::warp_sum(acc[s]);
+            if (lane == 0) atomicAdd(&cacc[sl * NLM + s], r);
+          }
+          pos = kend;
+          k++;
+        }
+      }
+      Kahan ka;
+      if (actA) {
+        // stencil weights scaled by 1/b_{k-1} (live in registers during this pass only)
+        float2 czs[O + 1], cxs[O + 1];
+#pragma unroll
+        for (int d = 1; d <= O; d++) {
+          czs[d] = splat(p.czf[d] * inv);
+          cxs[d] = ISO ? czs[d] : splat(p.cxf[d] * inv);
+        }
+        const int row4 = yA * nq + ql;  // quad index of (x0, yA) in a plane
+        const float4 *vrow = vq + (size_t)(K * p.EY + J + yA) * VRS4 + ql;
+        float4 ring[W];
+#pragma unroll
+        for (int q = -O; q < O; q++) {
+          const int zq = zbA + q;
+          ring[q + O + 1] = (zq >= 0 && zq < nz) ? P4c[row4 + zq * PS4] : zero4;
+        }
+        // x neighbours: the upper half of quad q-2, quads q-1 and q+1, the lower half of q+2
+        float2 xm2 = make_float2(0.f, 0.f), xp2 = make_float2(0.f, 0.f);
+        float4 xm1 = zero4, xp1 = zero4;
+        const float2 *P2c = reinterpret_cast<const float2 *>(P);
+        for (int z0 = zbA; z0 < zeA; z0 += W) {
+#pragma unroll
+          for (int s = 0; s < W; s++) {
+            const int z = z0 + s;
+            if (z >= zeA) break;
+            const int qn = z + O;
+            ring[s] = qn < nz ? P4c[row4 + qn * PS4] : zero4;
+#define RING(dd) ring[(s + (dd) + O + 1) % W]
+            const int i4 = row4 + z * PS4;
+            if (hm2) xm2 = P2c[2 * i4 - 3];
+            if (hm1) xm1 = P4c[i4 - 1];
+            if (hp1) xp1 = P4c[i4 + 1];
+            if (hp2) xp2 = P2c[2 * i4 + 4];
+            const float4 c = RING(0);
+            const float4 dv = __ldg(vrow + (size_t)z * VPS4);
+            const float2 vs01 = mul2(lo(c), inv2), vs23 = mul2(hi(c), inv2);  // v_k
+            float2 h01 = mul2(lo(dv), vs01), h23 = mul2(hi(dv), vs23);
+#pragma unroll
+            for (int d = 1; d <= O; d++) {
+              h01 = fma2(czs[d], add2(lo(RING(-d)), lo(RING(d))), h01);
+              h23 = fma2(czs[d], add2(hi(RING(-d)), hi(RING(d))), h23);
+            }
+#undef RING
+            // x neighbours: e[i] = P[x0 - 6 + i], i = 0..15
+            const float e[16] = {xm2.x, xm2.y, xm1.x, xm1.y, xm1.z, xm1.w, c.x,   c.y,
+                                 c.z,   c.w,   xp1.x, xp1.y, xp1.z, xp1.w, xp2.x, xp2.y};
+#pragma unroll
+            for (int d = 1; d <= O; d++) {
+              if (d % 2 == 0) {
+                h01 = fma2(cxs[d], add2(make_float2(e[6 - d], e[7 - d]), make_float2(e[6 + d], e[7 + d])), h01);
+                h23 = fma2(cxs[d], add2(make_float2(e[8 - d], e[9 - d]), make_float2(e[8 + d], e[9 + d])), h23);
+              } else {
+                h01 = fma2(cxs[d], make_float2(e[6 - d] + e[6 + d], e[7 - d] + e[7 + d]), h01);
+                h23 = fma2(cxs[d], make_float2(e[8 - d] + e[8 + d], e[9 - d] + e[9 + d]), h23);
+              }
+            }
+            // zero the pad points, U <- h - b_{k-1} U, a_k partial <v_k, h>
+            h01.y = in1 ? h01.y : 0.f;
+            h23.x = in2 ? h23.x : 0.f;
+            h23.y = in3 ? h23.y : 0.f;
+            const float4 uo = U4[i4];
+            const float2 n01 = fma2(ntb2, lo(uo), h01), n23 = fma2(ntb2, hi(uo), h23);
+            U4[i4] = make_float4(n01.x, n01.y, n23.x, n23.y);
+            const float2 pa = fma2(vs01, h01, mul2(vs23, h23));
+            ka.add(pa.x + pa.y);
+          }
+        }
+      }
+      __syncthreads();
+
+      // ---- phase 2: pass B  ||  alpha = Gamma c / b ----
+      if (actB) {
+        float2 cys[O + 1];
+#pragma unroll
+        for (int d = 1; d <= O; d++) cys[d] = splat((ISO ? p.czf[d] : p.cyf[d]) * inv);
+        const int pl4 = zB * PS4 + ql;  // quad index of (x0, y = 0) in plane zB
+        float4 ring[W];
+#pragma unroll
+        for (int q = -O; q < O; q++) {
+          const int yq = ybB + q;
+          ring[q + O + 1] = (yq >= 0 && yq < ny) ? P4c[pl4 + yq * nq] : zero4;
+        }
+        for (int y0 = ybB; y0 < yeB; y0 += W) {
+#pragma unroll
+          for (int s = 0; s < W; s++) {
+            const int y = y0 + s;
+            if (y >= yeB) break;
+            const int qn = y + O;
+            ring[s] = qn < ny ? P4c[pl4 + qn * nq] : zero4;
+#define RING(dd) ring[(s + (dd) + O + 1) % W]
+            float2 h01 = make_float2(0.f, 0.f), h23 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int d = 1; d <= O; d++) {
+              h01 = fma2(cys[d], add2(lo(RING(-d)), lo(RING(d))), h01);
+              h23 = fma2(cys[d], add2(hi(RING(-d)), hi(RING(d))), h23);
+            }
+            const float4 c = RING(0);
+#undef RING
+            const int u4 = pl4 + y * nq;
+            const float4 uo = U4[u4];
+            const float2 n01 = add2(lo(uo), h01), n23 = add2(hi(uo), h23);
+            U4[u4] = make_float4(n01.x, n01.y, n23.x, n23.y);
+            const float2 pa = fma2(mul2(lo(c), inv2), h01, mul2(mul2(hi(c), inv2), h23));
+            ka.add(pa.x + pa.y);
+          }
+        }
+      }
+      double a_part = (double)ka.s - (double)ka.c;
+      for (int e = threadIdx.x; e < n_slot * NLM; e += blockDim.x) {
+        const int sl = e / NLM, r = e - sl * NLM;
+        const TypeDesc &td = p.types[slot_type[sl]];
+        const int l = p.rank_l[r];
+        const double cv = (double)cacc[e] * (double)inv;
+        cacc[e] = 0.f;
+        const double gl = (td.chan_mask & (1 << l)) ? td.gamma[l] : 0.0;
+        alpha[e] = float(gl * cv);
+        a_part += gl * cv * cv;
+      }
+      a_part = lk::warp_sum(a_part);
+      if (lane == 0) red_a[warp] = a_part;
+      __syncthreads();
+
+      // ---- phase 3: projector scatter U += chi alpha  ||  a_k ----
+      {
+        int pos = r_begin, k = k_first;
+        while (pos < r_end) {
+          const int kend = min(r_end, koff[k + 1]);
+          const int shift = pref[k] - koff[k];
+          const float *al = alpha + slot[k] * NLM;
+          float coef[NLM];
+#pragma unroll
+          for (int s = 0; s < NLM; s++) coef[s] = al[s];
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
+            float c[kStream][NLM];
+            unsigned ix[kStream];
+#pragma unroll
+            for (int u = 0; u < kStream; u++) {
+              const int e = min(i0 + 32 * u, kend - 1) + shift;
+              ix[u] = ridx[e];
+              Rec::load(rec, e, c[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < kStream; u++) {
+              float val = 0.f;
+#pragma unroll
+              for (int s = 0; s < NLM; s++) val = fmaf(c[u][s], coef[s], val);
+              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u]], val);
+            }
+          }
+          pos = kend;
+          k++;
+        }
+      }
+      const double a = all_reduce(red_a, nw);
+      __syncthreads();
+
+      // ---- phase 4: w = U - a_k v, P <- w, U <- v, b_k^2 partial ----
+      {
+        const float2 na2 = splat(-float(a));
+        Kahan kb;
+        for (int e = threadIdx.x; e < (nc >> 2); e += blockDim.x) {
+          const float4 pv = P4[e], uv = U4[e];
+          const float2 v01 = mul2(lo(pv), inv2), v23 = mul2(hi(pv), inv2);
+          const float2 w01 = fma2(na2, v01, lo(uv)), w23 = fma2(na2, v23, hi(uv));
+          P4[e] = make_float4(w01.x, w01.y, w23.x, w23.y);
+          U4[e] = make_float4(v01.x, v01.y, v23.x, v23.y);
+          const float2 q = fma2(w01, w01, mul2(w23, w23));
+          kb.add(q.x + q.y);
+        }
+        double b_part = lk::warp_sum((double)kb.s - (double)kb.c);
+        if (lane == 0) red_b[warp] = b_part;
+        if (threadIdx.x == 0) sab[j] = a;
+      }
+      __syncthreads();
+      const double b = sqrt(all_reduce(red_b, nw));
+      if (threadIdx.x == 0) sab[64 + j] = b;
+      if (!(b > 0.0) || !isfinite(b)) {  // breakdown: the Krylov space is invariant
+        if (threadIdx.x == 0) {
+          atomicOr(status, kStatusBreakdown);
+          for (int r = j + 1; r < p.nqp; r++) {
+            sab[r] = 0.0;
+            sab[64 + r] = 0.0;
+          }
+        }
+        break;
+      }
+      beta = b;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < p.nqp; r += blockDim.x) {
+      double *o = ab_out + (node - p.node_begin) * 2 * p.nqp;
+      o[r] = sab[r];
+      o[p.nqp + r] = sab[64 + r];
+    }
+    __syncthreads();
+  }
+}
+
+template <int MASK, int MAXT, bool ISO>
+cudaError_t launch_quad_variant(const LanczosParams &p, int grid, int block, size_t smem,
+                                cudaStream_t s, const void *veffq, const ImageMeta *images,
+                                const void *tables, void *proj_scratch, double *ab, int *status) {
+  if (block > MAXT) return cudaErrorInvalidConfiguration;
+  auto k = lanczos_quad_kernel<MASK, MAXT, ISO>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, block, smem, s>>>(p, (const float *)veffq, images, (const float *)tables,
+                              (unsigned char *)proj_scratch, ab, status);
+  return cudaGetLastError();
+}
+
+}  // namespace lq
+}  // namespace sq

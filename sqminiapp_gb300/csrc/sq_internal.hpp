@@ -64,6 +64,9 @@ struct LanczosParams {
   int rank_l[kMaxLm];      // l of compact slot r
   int ntype;
   int rows_per_warp;       // cube y-rows owned by one warp in the vector passes
+  int zchunks;             // kLayoutQuad: z-ranges (pass A) and y-ranges (pass B) per row / plane
+  int vq_row;              // kLayoutQuad: row length (floats) of the quad-aligned Veff copies
+  long long vq_copy_stride;  // kLayoutQuad: floats per quad-aligned Veff copy
   int proj_cap;            // records of one CTA's projector list (max box points of a node)
   long long proj_bytes_per_cta;
   long long node_begin, node_end;

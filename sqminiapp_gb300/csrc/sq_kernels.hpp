@@ -23,6 +23,10 @@ constexpr int kLayoutXClamp = 4;  // FP64: rows without zero columns, x bounds-c
 // coordinates (12 B for s+p) instead of chi_lm and packed P|U indices (20 B); chi_lm is
 // rebuilt from the solid harmonics while streaming.  For lists that would not stay in L2.
 constexpr int kLayoutCompact = 8;
+// FP32, corrected operator, cubes at most 32 points wide, P and U on chip: split stencil passes
+// over 16-byte quads (lanczos_quad.cuh); rows of 4*ceil(nx/4) floats, no gaps.
+constexpr int kLayoutQuad = 16;
+constexpr int kQuadMaxThreads = 512;
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;
@@ -47,6 +51,12 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
 
 cudaError_t launch_veff_extend(const double *veff, double vconst, void *ext, int precision,
                                const LanczosParams &p, cudaStream_t s);
+
+// kLayoutQuad: the four quad-aligned copies of cdiag + Veff padded periodically by the cube
+// half-width (copy s holds extended x index ex at row position ex + s; rows of vq_row floats).
+size_t veff_quad_floats(const LanczosParams &p);
+size_t lanczos_quad_smem_bytes(const LanczosParams &p);
+int lanczos_quad_threads(const LanczosParams &p);
 
 // Implicit QL of every node's tridiagonal; ab = [n][2][nqp] (a then b).
 cudaError_t launch_quadrature(const double *ab, long long n, int nqp, double *lambda, double *w,

@@ -6,7 +6,7 @@ import pytest
 from sqminiapp_gb300 import GB300_DEVICE, SqError, plan_kernel
 from sqminiapp_gb300.decks import CONFIGS, make_fcc_mg_deck
 
-YGAP, WIDE, XCLAMP, COMPACT = 1, 2, 4, 8
+YGAP, WIDE, XCLAMP, COMPACT, QUAD = 1, 2, 4, 8, 16
 
 
 @pytest.fixture(scope="module")
@@ -25,25 +25,52 @@ def _plan(decks, name, **kw):
 
 def test_fp32_layouts(decks):
     smem_max = GB300_DEVICE["smem_optin"]
-    p = _plan(decks, "mg32_h0.5_rc6.5_q40")  # 27^3: y gaps, U on chip, 14 warps, full list
-    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP, 1, 448)
-    p = _plan(decks, "uneven_a_mg4_h0.5_rc6_q30")  # 25^3
-    assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 1)
-    p = _plan(decks, "mg500_h0.5_rc7_q50")  # 29^3: U on chip only without the y gaps
-    assert (p.kernel_layout, p.kernel_u_on_chip) == (0, 1)
+    # the split-pass kernel wherever it applies: rows of 4*ceil(n/4) floats, P and U on chip,
+    # ceil(n/4) threads per row times two z-ranges (the default tile before autotuning)
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40")  # 27^3: 7 quads x 27 rows x 2 = 378 -> 384
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (QUAD, 1, 384)
+    p = _plan(decks, "uneven_a_mg4_h0.5_rc6_q30")  # 25^3: 350 -> 352
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (QUAD, 1, 352)
+    p = _plan(decks, "mg500_h0.5_rc7_q50")  # 29^3: 8 quads x 29 x 2 = 464 -> 480
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (QUAD, 1, 480)
     p = _plan(decks, "uneven_b_mg32_h0.45_rc7_q40")  # 33^3: wide, U in L2, compact list
     assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP | WIDE | COMPACT, 0, 576)
     for name in decks:
         assert 0 < _plan(decks, name).kernel_smem_bytes <= smem_max
 
 
+def test_single_pass_kernel_layouts(decks):
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40", kernel=1)  # 27^3: y gaps, U on chip, 14 warps
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP, 1, 448)
+    p = _plan(decks, "uneven_a_mg4_h0.5_rc6_q30", kernel=1)  # 25^3
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 1)
+    p = _plan(decks, "mg500_h0.5_rc7_q50", kernel=1)  # 29^3: U on chip only without the y gaps
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (0, 1)
+
+
+def test_kernel_option(decks):
+    # the split-pass kernel on request, with a chosen tile; refused where it does not apply
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40", kernel=2, tile=1)
+    assert (p.kernel_layout, p.kernel_threads) == (QUAD, 192)
+    for kw in ({"faithful": True}, {"precision": 64}, {"list_format": 2}):
+        with pytest.raises(SqError):
+            _plan(decks, "mg32_h0.5_rc6.5_q40", kernel=2, **kw)
+    with pytest.raises(SqError):
+        _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", kernel=2)  # 33 points wide
+    with pytest.raises(SqError):
+        _plan(decks, "mg32_h0.5_rc6.5_q40", kernel=3)
+    # a tile whose threads exceed the kernel's 512 falls back to the single-pass kernel
+    assert _plan(decks, "mg32_h0.5_rc6.5_q40", tile=3).kernel_layout == YGAP
+
+
 def test_list_format_option(decks):
     assert _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", list_format=1).kernel_layout == YGAP | WIDE
     assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2).kernel_layout == YGAP | COMPACT
+    assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=1).kernel_layout == QUAD
     # the faithful operator and FP64 keep the full records
     assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2, faithful=True).kernel_layout == YGAP
     assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2, precision=64).kernel_layout == 0
-    # a small L2 turns the automatic choice to compact records
+    # a small L2 turns the automatic choice to the single-pass kernel with compact records
     small = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"l2_bytes": 16 << 20})
     assert small.kernel_layout == YGAP | COMPACT
     with pytest.raises(SqError):
@@ -63,5 +90,7 @@ def test_fp64_layouts(decks):
 def test_smaller_shared_memory_moves_u_off_chip(decks):
     p = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 160 * 1024})
     assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 0)
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 170 * 1024})
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (QUAD, 1)
     with pytest.raises(SqError):
         _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 64 * 1024})

@@ -1,6 +1,7 @@
-"""The Lanczos kernel's on-chip index arithmetic, restated on the CPU for every cube size the
-engine accepts, in the layout sq_plan_kernel picks for it (the same host code the engine
-runs): every stencil read of P lands either on the right neighbour's slot or, where that
+"""The single-pass Lanczos kernel's on-chip index arithmetic, restated on the CPU for every
+cube size the engine accepts, in the layout sq_plan_kernel picks for it with kernel=1 (the same
+host code the engine runs; the split-pass kernel has its own restatement in
+test_quad_layout.py): every stencil read of P lands either on the right neighbour's slot or, where that
 neighbour is outside the cube, on a slot that is never written (a zero pad column, a zero gap
 row, or the leading offset) or is masked by a bounds check; every index stays inside the
 buffers and fits the 16-bit packing of the projector records.
@@ -90,10 +91,10 @@ def test_kernel_index_arithmetic_stays_in_bounds(rcut, h, precision, fits, tmp_p
     d, name, _ = make_fcc_mg_deck(str(tmp_path), "c", ncell=1, h=h, rcut=rcut, n_qp=20)
     if not fits:
         with pytest.raises(Exception) as e:
-            plan_kernel(d, name, precision=precision)
+            plan_kernel(d, name, precision=precision, kernel=1)
         assert "does not fit" in str(e.value) or "FP32" in str(e.value)
         return
-    p = plan_kernel(d, name, precision=precision)
+    p = plan_kernel(d, name, precision=precision, kernel=1)
     n = p.cube[0]
     assert n == 2 * int(np.ceil(rcut / h - 1e-12)) + 1
     flags = p.kernel_layout & 7
