@@ -6,8 +6,9 @@ namespace sq {
 
 int lanczos_quad_threads(const LanczosParams &p) {
   // pitch/4 threads per row (pass A) or plane (pass B), zchunks ranges each
+  // at least two warps: warp 0 builds the per-node image list while the others clear P and U
   const int groups = std::max(p.ny, p.nz) * p.zchunks;
-  return 32 * (((p.pitch / 4) * groups + 31) / 32);
+  return std::max(64, 32 * (((p.pitch / 4) * groups + 31) / 32));
 }
 
 size_t lanczos_quad_smem_bytes(const LanczosParams &p) {

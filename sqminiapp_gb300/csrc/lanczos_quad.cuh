@@ -23,14 +23,22 @@
 // Eight consecutive threads own the quads of one row (pass A) or one plane (pass B), so a
 // quarter-warp's float4 accesses cover one contiguous row: no bank conflicts.
 //
+// Projector list: as in lanczos_kernel.cuh (chi_lm of the node's support points, built once
+// per node into the CTA's slice of global scratch), with one index per point (P and U share
+// it) and every image's records padded with zero records to a multiple of four, so a lane
+// streams four consecutive points with one 16-byte index load and four 16-byte record loads.
+//
 // Per Lanczos step (P = b v_k unnormalised, U = v_{k-1}), four CTA barriers:
 //   1  projector gather c = chi^T P (per-warp ranges of the node's list)  ||  pass A
 //   2  pass B  ||  alpha = Gamma c / b (and <v, V_nl v>)  -> per-warp partials of a_k
 //   3  projector scatter U += chi alpha  ||  every warp reduces the a_k partials
 //   4  w = U - a_k v, P <- w, U <- v  -> per-warp partials of b_k^2
-// After barrier 4 every warp reduces the b partials itself (the same FP64 tree in every warp,
-// so every thread sees the same b_k and takes the same branch).  a_k and b_k^2 are summed per
-// thread in FP32 with Kahan compensation, then across threads in FP64.
+// After barrier 4 every warp reduces the b partials itself (the same tree in every warp, so
+// every thread sees the same b_k and takes the same branch).  a_k and b_k^2 are summed per
+// thread in FP32 with Kahan compensation, then across threads as double-float pairs (an FP32
+// head and tail added with error-free transformations, about 48 bits of significand): GB300's
+// FP64 pipe runs at a small fraction of its FP32 rate, so the step loop keeps FP64 out of its
+// critical path and converts to double only to store a_k and b_k.
 #pragma once
 
 #include "lanczos_kernel.cuh"
@@ -79,14 +87,39 @@ struct Kahan {
   }
 };
 
-// Sum of the kMaxWarps-entry array of per-warp partials (nw of them), the same FP64 butterfly
-// in every lane of every warp, so every thread gets the bit-identical total.
-__device__ __forceinline__ double all_reduce(const double *red, int nw) {
-  const int lane = threadIdx.x & 31;
-  double v = lane < nw ? red[lane] : 0.0;
+// Double-float value hi + lo (|lo| <= ulp(hi)/2) and its sum (Knuth's TwoSum, then a
+// renormalising FastTwoSum).
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  const float s = x.hi + y.hi;
+  const float bb = s - x.hi;
+  float e = (x.hi - (s - bb)) + (y.hi - bb);
+  e += x.lo + y.lo;
+  const float h = s + e;
+  return DF{h, e - (h - s)};
+}
+__device__ __forceinline__ DF df_of(const Kahan &k) {  // s - c, renormalised
+  const float h = k.s - k.c;
+  return DF{h, -k.c - (h - k.s)};
+}
+__device__ __forceinline__ DF df_warp_sum(DF v) {  // the same butterfly in every lane
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    DF w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = df_add(v, w);
+  }
   return v;
+}
+// Sum of nw per-warp partials red[0..nw), the same tree in every lane of every warp, so every
+// thread gets the bit-identical total.
+__device__ __forceinline__ DF df_all_reduce(const float2 *red, int nw) {
+  const int lane = threadIdx.x & 31;
+  const float2 r = lane < nw ? red[lane] : make_float2(0.f, 0.f);
+  return df_warp_sum(DF{r.x, r.y});
 }
 
 template <int MASK, int MAXT, bool ISO>
@@ -97,7 +130,9 @@ __global__ void __launch_bounds__(MAXT, 1)
                         int *__restrict__ status) {
   constexpr int NLM = lk::Lm<MASK>::nlm;
   using Rec = lk::ProjRec<float, NLM>;
-  constexpr int kStream = lk::stream_batch<Rec::nvec * (int)sizeof(typename Rec::vec_t)>();
+  // groups of four points per lane per batch of the projector streams (records of up to 16
+  // bytes: two groups, eight points in flight per lane)
+  constexpr int kStream4 = Rec::nvec * (int)sizeof(typename Rec::vec_t) <= 16 ? 2 : 1;
   const int nw = blockDim.x >> 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
@@ -111,9 +146,9 @@ __global__ void __launch_bounds__(MAXT, 1)
   float *P = reinterpret_cast<float *>(smem_raw);
   float *U = P + nc;
   unsigned char *cur = reinterpret_cast<unsigned char *>(U + nc);
-  double *red_a = reinterpret_cast<double *>(cur);
-  double *red_b = red_a + kMaxWarps;
-  double *sab = red_b + kMaxWarps;  // a[64], b[64]
+  double *sab = reinterpret_cast<double *>(cur);  // a[64], b[64]
+  float2 *red_a = reinterpret_cast<float2 *>(sab + 128);  // per-warp double-float partials
+  float2 *red_b = red_a + kMaxWarps;
   cur += sizeof(double) * (2 * kMaxWarps + 128);
   float *cacc = reinterpret_cast<float *>(cur);
   cur += sizeof(float) * maxi * NLM;
@@ -133,6 +168,7 @@ __global__ void __launch_bounds__(MAXT, 1)
       proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
   unsigned *ridx = reinterpret_cast<unsigned *>(
       reinterpret_cast<unsigned char *>(rec) + (size_t)p.proj_cap * sizeof(typename Rec::vec_t) * Rec::nvec);
+  const uint4 *ridx4 = reinterpret_cast<const uint4 *>(ridx);
 
   const float4 *P4c = reinterpret_cast<const float4 *>(P);
   float4 *P4 = reinterpret_cast<float4 *>(P);
@@ -205,7 +241,8 @@ __global__ void __launch_bounds__(MAXT, 1)
         }
         const unsigned m = __ballot_sync(0xffffffffu, start);
         const int g = slots + __popc(m & ((1u << lane) - 1u)) + (start ? 0 : -1);
-        int incl = npts;
+        const int npts4 = (npts + 3) & ~3;  // room for the padding of the kept points
+        int incl = npts4;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const int t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -216,7 +253,7 @@ __global__ void __launch_bounds__(MAXT, 1)
           if (start) slot_type[g] = type;
           blo[k] = lo;
           bext[k] = ext;
-          pref[k] = offset + incl - npts;
+          pref[k] = offset + incl - npts4;
         }
         slots += __popc(m);
         offset += __shfl_sync(0xffffffffu, incl, 31);
@@ -249,7 +286,7 @@ __global__ void __launch_bounds__(MAXT, 1)
     for (int kk = warp; kk < n_img; kk += nw) {
       const lk::ImgView<float> v =
           lk::load_view<float>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, 0, PS);
-      const int npts = pref[kk + 1] - pref[kk];
+      const int npts = v.ex * v.ey * ((bext[kk] >> 20) & 1023);
       int kept_n = 0;
       for (int q0 = 0; q0 < npts; q0 += 32) {
         const int q = q0 + lane;
@@ -286,7 +323,16 @@ __global__ void __launch_bounds__(MAXT, 1)
         }
         kept_n += __popc(m);
       }
-      if (lane == 0) kept[kk] = kept_n;
+      // zero records up to a multiple of four (index 0: a real point; they add nothing)
+      const int kept4 = (kept_n + 3) & ~3;
+      if (lane < kept4 - kept_n) {
+        float zero[Rec::n];
+#pragma unroll
+        for (int s = 0; s < Rec::n; s++) zero[s] = 0.f;
+        Rec::store(rec, pref[kk] + kept_n + lane, zero);
+        ridx[pref[kk] + kept_n + lane] = 0u;
+      }
+      if (lane == 0) kept[kk] = kept4;
     }
     __syncthreads();
     if (warp == 0) {  // exclusive scan of kept -> koff
@@ -306,8 +352,8 @@ __global__ void __launch_bounds__(MAXT, 1)
       if (lane == 0) koff[n_img] = offset;
     }
     __syncthreads();
-    const int total = koff[n_img];
-    const int per = (total + nw - 1) / nw;
+    const int total = koff[n_img];  // a multiple of four, as every image's share
+    const int per = 4 * ((total + 4 * nw - 1) / (4 * nw));
     const int r_begin = min(total, warp * per), r_end = min(total, r_begin + per);
     int k_first = 0;  // image holding kept point r_begin: largest k with koff[k] <= r_begin
     {
@@ -327,10 +373,9 @@ __global__ void __launch_bounds__(MAXT, 1)
     const size_t VPS4 = (size_t)p.EY * (p.vq_row >> 2);  // plane stride in quads
     const size_t VRS4 = (size_t)(p.vq_row >> 2);         // row stride in quads
 
-    double beta = 1.0;
+    float tb = 1.f;  // b_{k-1}
     for (int j = 0; j < p.nqp; j++) {
-      const float inv = float(1.0 / beta);
-      const float tb = float(beta);
+      const float inv = 1.f / tb;
       const float2 inv2 = splat(inv), ntb2 = splat(-tb);
 
       // ---- phase 1: projector gather  ||  pass A ----
@@ -338,24 +383,31 @@ __global__ void __launch_bounds__(MAXT, 1)
         int pos = r_begin, k = k_first;
         while (pos < r_end) {
           const int kend = min(r_end, koff[k + 1]);
-          const int shift = pref[k] - koff[k];
+          const int shift = pref[k] - koff[k];  // a multiple of four
           float acc[NLM];
 #pragma unroll
           for (int s = 0; s < NLM; s++) acc[s] = 0.f;
-          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
-            float c[kStream][NLM];
-            unsigned ix[kStream];
+          // four consecutive points per lane, kStream4 groups per lane in flight
+          for (int g0 = pos + 4 * lane; g0 < kend; g0 += 128 * kStream4) {
+            float c[kStream4][4][NLM];
+            uint4 ix[kStream4];
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
-              const int e = min(i0 + 32 * u, kend - 1) + shift;
-              ix[u] = ridx[e];
-              Rec::load(rec, e, c[u]);
+            for (int u = 0; u < kStream4; u++) {
+              const int e = min(g0 + 128 * u, kend - 4) + shift;
+              ix[u] = ridx4[e >> 2];
+#pragma unroll
+              for (int t = 0; t < 4; t++) Rec::load(rec, e + t, c[u][t]);
             }
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
-              const float val = (i0 + 32 * u < kend) ? P[ix[u]] : 0.f;
+            for (int u = 0; u < kStream4; u++) {
+              const bool ok = g0 + 128 * u < kend;
+              const unsigned ii[4] = {ix[u].x, ix[u].y, ix[u].z, ix[u].w};
 #pragma unroll
-              for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][s], val, acc[s]);
+              for (int t = 0; t < 4; t++) {
+                const float val = ok ? P[ii[t]] : 0.f;
+#pragma unroll
+                for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][t][s], val, acc[s]);
+              }
             }
           }
           const int sl = slot[k];
@@ -476,19 +528,22 @@ __global__ void __launch_bounds__(MAXT, 1)
           }
         }
       }
-      double a_part = (double)ka.s - (double)ka.c;
+      // alpha = Gamma_l c, with c = <chi, v_k>; <v_k, V_nl v_k> = sum Gamma_l c^2 joins a_k
       for (int e = threadIdx.x; e < n_slot * NLM; e += blockDim.x) {
         const int sl = e / NLM, r = e - sl * NLM;
         const TypeDesc &td = p.types[slot_type[sl]];
         const int l = p.rank_l[r];
-        const double cv = (double)cacc[e] * (double)inv;
+        const float cv = cacc[e] * inv;
         cacc[e] = 0.f;
-        const double gl = (td.chan_mask & (1 << l)) ? td.gamma[l] : 0.0;
-        alpha[e] = float(gl * cv);
-        a_part += gl * cv * cv;
+        const float gl = (td.chan_mask & (1 << l)) ? float(td.gamma[l]) : 0.f;
+        const float al = gl * cv;
+        alpha[e] = al;
+        ka.add(al * cv);
       }
-      a_part = lk::warp_sum(a_part);
-      if (lane == 0) red_a[warp] = a_part;
+      {
+        const DF ap = df_warp_sum(df_of(ka));
+        if (lane == 0) red_a[warp] = make_float2(ap.hi, ap.lo);
+      }
       __syncthreads();
 
       // ---- phase 3: projector scatter U += chi alpha  ||  a_k ----
@@ -501,33 +556,40 @@ __global__ void __launch_bounds__(MAXT, 1)
           float coef[NLM];
 #pragma unroll
           for (int s = 0; s < NLM; s++) coef[s] = al[s];
-          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
-            float c[kStream][NLM];
-            unsigned ix[kStream];
+          for (int g0 = pos + 4 * lane; g0 < kend; g0 += 128 * kStream4) {
+            float c[kStream4][4][NLM];
+            uint4 ix[kStream4];
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
-              const int e = min(i0 + 32 * u, kend - 1) + shift;
-              ix[u] = ridx[e];
-              Rec::load(rec, e, c[u]);
+            for (int u = 0; u < kStream4; u++) {
+              const int e = min(g0 + 128 * u, kend - 4) + shift;
+              ix[u] = ridx4[e >> 2];
+#pragma unroll
+              for (int t = 0; t < 4; t++) Rec::load(rec, e + t, c[u][t]);
             }
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
-              float val = 0.f;
+            for (int u = 0; u < kStream4; u++) {
+              if (g0 + 128 * u < kend) {
+                const unsigned ii[4] = {ix[u].x, ix[u].y, ix[u].z, ix[u].w};
 #pragma unroll
-              for (int s = 0; s < NLM; s++) val = fmaf(c[u][s], coef[s], val);
-              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u]], val);
+                for (int t = 0; t < 4; t++) {
+                  float val = 0.f;
+#pragma unroll
+                  for (int s = 0; s < NLM; s++) val = fmaf(c[u][t][s], coef[s], val);
+                  atomicAdd(&U[ii[t]], val);
+                }
+              }
             }
           }
           pos = kend;
           k++;
         }
       }
-      const double a = all_reduce(red_a, nw);
+      const DF adf = df_all_reduce(red_a, nw);
       __syncthreads();
 
       // ---- phase 4: w = U - a_k v, P <- w, U <- v, b_k^2 partial ----
       {
-        const float2 na2 = splat(-float(a));
+        const float2 na2 = splat(-(adf.hi + adf.lo));
         Kahan kb;
         for (int e = threadIdx.x; e < (nc >> 2); e += blockDim.x) {
           const float4 pv = P4[e], uv = U4[e];
@@ -538,14 +600,15 @@ __global__ void __launch_bounds__(MAXT, 1)
           const float2 q = fma2(w01, w01, mul2(w23, w23));
           kb.add(q.x + q.y);
         }
-        double b_part = lk::warp_sum((double)kb.s - (double)kb.c);
-        if (lane == 0) red_b[warp] = b_part;
-        if (threadIdx.x == 0) sab[j] = a;
+        const DF bp = df_warp_sum(df_of(kb));
+        if (lane == 0) red_b[warp] = make_float2(bp.hi, bp.lo);
+        if (threadIdx.x == 0) sab[j] = (double)adf.hi + (double)adf.lo;
       }
       __syncthreads();
-      const double b = sqrt(all_reduce(red_b, nw));
-      if (threadIdx.x == 0) sab[64 + j] = b;
-      if (!(b > 0.0) || !isfinite(b)) {  // breakdown: the Krylov space is invariant
+      const DF b2 = df_all_reduce(red_b, nw);
+      const float bf = sqrtf(b2.hi + b2.lo);
+      if (threadIdx.x == 0) sab[64 + j] = sqrt((double)b2.hi + (double)b2.lo);
+      if (!(bf > 0.f) || !isfinite(bf)) {  // breakdown: the Krylov space is invariant
         if (threadIdx.x == 0) {
           atomicOr(status, kStatusBreakdown);
           for (int r = j + 1; r < p.nqp; r++) {
@@ -555,7 +618,7 @@ __global__ void __launch_bounds__(MAXT, 1)
         }
         break;
       }
-      beta = b;
+      tb = bf;
     }
     __syncthreads();
     for (int r = threadIdx.x; r < p.nqp; r += blockDim.x) {

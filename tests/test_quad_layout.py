@@ -21,7 +21,24 @@ MAX_THREADS = 512
 
 def quad_threads(n, tile):
     nq = (n + 3) // 4
-    return 32 * ((nq * n * tile + 31) // 32)
+    return max(64, 32 * ((nq * n * tile + 31) // 32))
+
+
+@pytest.mark.parametrize("n,h", [(3, 0.85), (5, 0.85), (9, 0.85), (17, 0.5), (27, 0.5)])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+def test_engine_thread_count(n, h, tile, tmp_path):
+    """The engine's thread count for a tile (sq_plan_kernel) is the restated one, and always
+    at least two warps: warp 0 builds a node's image list while the others clear P and U."""
+    from sqminiapp_gb300 import plan_kernel
+    from sqminiapp_gb300.decks import make_fcc_mg_deck
+    rcut = h * (n - 1) / 2
+    d, name, _ = make_fcc_mg_deck(str(tmp_path), "c", ncell=1, h=h, rcut=rcut, n_qp=8)
+    want = quad_threads(n, tile)
+    if want > MAX_THREADS:
+        return
+    p = plan_kernel(d, name, kernel=2, tile=tile)
+    assert p.cube[0] == n
+    assert p.kernel_threads == want >= 64
 
 
 def thread_maps(n, tile):
