@@ -387,8 +387,7 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
     if (psize >= 65536 || (long long)p.upitch * p.ny * p.nz >= 65536)
       throw std::invalid_argument("truncated cube too large for 16-bit point indices");
   }
-  // the split-pass kernel pads every image's kept points to a multiple of four
-  const long long cap = std::max(1LL, max_box_points_per_node(s, d)) + (h->quad ? 3LL * p.max_img : 0LL);
+  const long long cap = std::max(1LL, max_box_points_per_node(s, d));
   if (cap > (1LL << 31) - 1) throw std::invalid_argument("projector list too large");
   p.proj_cap = (int)cap;
   p.proj_bytes_per_cta =

@@ -25,8 +25,8 @@
 //
 // Projector list: as in lanczos_kernel.cuh (chi_lm of the node's support points, built once
 // per node into the CTA's slice of global scratch), with one index per point (P and U share
-// it) and every image's records padded with zero records to a multiple of four, so a lane
-// streams four consecutive points with one 16-byte index load and four 16-byte record loads.
+// it); consecutive lanes stream consecutive points, so every record load of a warp is one
+// contiguous 512-byte run.
 //
 // Per Lanczos step (P = b v_k unnormalised, U = v_{k-1}), four CTA barriers:
 //   1  projector gather c = chi^T P (per-warp ranges of the node's list)  ||  pass A
@@ -130,9 +130,7 @@ __global__ void __launch_bounds__(MAXT, 1)
                         int *__restrict__ status) {
   constexpr int NLM = lk::Lm<MASK>::nlm;
   using Rec = lk::ProjRec<float, NLM>;
-  // groups of four points per lane per batch of the projector streams (records of up to 16
-  // bytes: two groups, eight points in flight per lane)
-  constexpr int kStream4 = Rec::nvec * (int)sizeof(typename Rec::vec_t) <= 16 ? 2 : 1;
+  constexpr int kStream = lk::stream_batch<Rec::nvec * (int)sizeof(typename Rec::vec_t)>();
   const int nw = blockDim.x >> 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
@@ -168,7 +166,6 @@ __global__ void __launch_bounds__(MAXT, 1)
       proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
   unsigned *ridx = reinterpret_cast<unsigned *>(
       reinterpret_cast<unsigned char *>(rec) + (size_t)p.proj_cap * sizeof(typename Rec::vec_t) * Rec::nvec);
-  const uint4 *ridx4 = reinterpret_cast<const uint4 *>(ridx);
 
   const float4 *P4c = reinterpret_cast<const float4 *>(P);
   float4 *P4 = reinterpret_cast<float4 *>(P);
@@ -241,8 +238,7 @@ __global__ void __launch_bounds__(MAXT, 1)
         }
         const unsigned m = __ballot_sync(0xffffffffu, start);
         const int g = slots + __popc(m & ((1u << lane) - 1u)) + (start ? 0 : -1);
-        const int npts4 = (npts + 3) & ~3;  // room for the padding of the kept points
-        int incl = npts4;
+        int incl = npts;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const int t = __shfl_up_sync(0xffffffffu, incl, o);
@@ -253,7 +249,7 @@ __global__ void __launch_bounds__(MAXT, 1)
           if (start) slot_type[g] = type;
           blo[k] = lo;
           bext[k] = ext;
-          pref[k] = offset + incl - npts4;
+          pref[k] = offset + incl - npts;
         }
         slots += __popc(m);
         offset += __shfl_sync(0xffffffffu, incl, 31);
@@ -286,7 +282,7 @@ __global__ void __launch_bounds__(MAXT, 1)
     for (int kk = warp; kk < n_img; kk += nw) {
       const lk::ImgView<float> v =
           lk::load_view<float>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, 0, PS);
-      const int npts = v.ex * v.ey * ((bext[kk] >> 20) & 1023);
+      const int npts = pref[kk + 1] - pref[kk];
       int kept_n = 0;
       for (int q0 = 0; q0 < npts; q0 += 32) {
         const int q = q0 + lane;
@@ -323,16 +319,7 @@ __global__ void __launch_bounds__(MAXT, 1)
         }
         kept_n += __popc(m);
       }
-      // zero records up to a multiple of four (index 0: a real point; they add nothing)
-      const int kept4 = (kept_n + 3) & ~3;
-      if (lane < kept4 - kept_n) {
-        float zero[Rec::n];
-#pragma unroll
-        for (int s = 0; s < Rec::n; s++) zero[s] = 0.f;
-        Rec::store(rec, pref[kk] + kept_n + lane, zero);
-        ridx[pref[kk] + kept_n + lane] = 0u;
-      }
-      if (lane == 0) kept[kk] = kept4;
+      if (lane == 0) kept[kk] = kept_n;
     }
     __syncthreads();
     if (warp == 0) {  // exclusive scan of kept -> koff
@@ -352,8 +339,8 @@ __global__ void __launch_bounds__(MAXT, 1)
       if (lane == 0) koff[n_img] = offset;
     }
     __syncthreads();
-    const int total = koff[n_img];  // a multiple of four, as every image's share
-    const int per = 4 * ((total + 4 * nw - 1) / (4 * nw));
+    const int total = koff[n_img];
+    const int per = (total + nw - 1) / nw;
     const int r_begin = min(total, warp * per), r_end = min(total, r_begin + per);
     int k_first = 0;  // image holding kept point r_begin: largest k with koff[k] <= r_begin
     {
@@ -383,31 +370,24 @@ __global__ void __launch_bounds__(MAXT, 1)
         int pos = r_begin, k = k_first;
         while (pos < r_end) {
           const int kend = min(r_end, koff[k + 1]);
-          const int shift = pref[k] - koff[k];  // a multiple of four
+          const int shift = pref[k] - koff[k];
           float acc[NLM];
 #pragma unroll
           for (int s = 0; s < NLM; s++) acc[s] = 0.f;
-          // four consecutive points per lane, kStream4 groups per lane in flight
-          for (int g0 = pos + 4 * lane; g0 < kend; g0 += 128 * kStream4) {
-            float c[kStream4][4][NLM];
-            uint4 ix[kStream4];
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
+            float c[kStream][NLM];
+            unsigned ix[kStream];
 #pragma unroll
-            for (int u = 0; u < kStream4; u++) {
-              const int e = min(g0 + 128 * u, kend - 4) + shift;
-              ix[u] = ridx4[e >> 2];
-#pragma unroll
-              for (int t = 0; t < 4; t++) Rec::load(rec, e + t, c[u][t]);
+            for (int u = 0; u < kStream; u++) {
+              const int e = min(i0 + 32 * u, kend - 1) + shift;
+              ix[u] = ridx[e];
+              Rec::load(rec, e, c[u]);
             }
 #pragma unroll
-            for (int u = 0; u < kStream4; u++) {
-              const bool ok = g0 + 128 * u < kend;
-              const unsigned ii[4] = {ix[u].x, ix[u].y, ix[u].z, ix[u].w};
+            for (int u = 0; u < kStream; u++) {
+              const float val = (i0 + 32 * u < kend) ? P[ix[u]] : 0.f;
 #pragma unroll
-              for (int t = 0; t < 4; t++) {
-                const float val = ok ? P[ii[t]] : 0.f;
-#pragma unroll
-                for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][t][s], val, acc[s]);
-              }
+              for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][s], val, acc[s]);
             }
           }
           const int sl = slot[k];
@@ -556,28 +536,21 @@ __global__ void __launch_bounds__(MAXT, 1)
           float coef[NLM];
 #pragma unroll
           for (int s = 0; s < NLM; s++) coef[s] = al[s];
-          for (int g0 = pos + 4 * lane; g0 < kend; g0 += 128 * kStream4) {
-            float c[kStream4][4][NLM];
-            uint4 ix[kStream4];
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
+            float c[kStream][NLM];
+            unsigned ix[kStream];
 #pragma unroll
-            for (int u = 0; u < kStream4; u++) {
-              const int e = min(g0 + 128 * u, kend - 4) + shift;
-              ix[u] = ridx4[e >> 2];
-#pragma unroll
-              for (int t = 0; t < 4; t++) Rec::load(rec, e + t, c[u][t]);
+            for (int u = 0; u < kStream; u++) {
+              const int e = min(i0 + 32 * u, kend - 1) + shift;
+              ix[u] = ridx[e];
+              Rec::load(rec, e, c[u]);
             }
 #pragma unroll
-            for (int u = 0; u < kStream4; u++) {
-              if (g0 + 128 * u < kend) {
-                const unsigned ii[4] = {ix[u].x, ix[u].y, ix[u].z, ix[u].w};
+            for (int u = 0; u < kStream; u++) {
+              float val = 0.f;
 #pragma unroll
-                for (int t = 0; t < 4; t++) {
-                  float val = 0.f;
-#pragma unroll
-                  for (int s = 0; s < NLM; s++) val = fmaf(c[u][t][s], coef[s], val);
-                  atomicAdd(&U[ii[t]], val);
-                }
-              }
+              for (int s = 0; s < NLM; s++) val = fmaf(c[u][s], coef[s], val);
+              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u]], val);
             }
           }
           pos = kend;
