@@ -16,8 +16,8 @@ size_t lanczos_quad_smem_bytes(const LanczosParams &p) {
   const int nlm = mask_nlm(kernel_mask(p.union_mask));
   size_t b = sizeof(float) * 2 * nc;                          // P, U
   b += sizeof(double) * (2 * lk::kMaxWarps + 128);           // a_k / b_k partials, a[], b[]
-  b += sizeof(float) * 2 * (size_t)p.max_img * nlm;           // gathered c, alpha
-  b += sizeof(int) * (8 * (size_t)p.max_img + 2) + sizeof(int) * 4;  // per-node image lists
+  b += sizeof(float) * (2 * (size_t)p.max_img + lk::kMaxWarps) * nlm;  // c partials, alpha
+  b += sizeof(int) * (9 * (size_t)p.max_img + 2) + sizeof(int) * 4;    // per-node image lists
   return b;
 }
 

@@ -29,9 +29,11 @@
 // contiguous 512-byte run.
 //
 // Per Lanczos step (P = b v_k unnormalised, U = v_{k-1}), four CTA barriers:
-//   1  projector gather c = chi^T P (per-warp ranges of the node's list)  ||  pass A
+//   1  projector gather c = chi^T P (per-warp ranges of the node's list, one partial per
+//      warp and image, no atomics)  ||  pass A
 //   2  pass B  ||  alpha = Gamma c / b (and <v, V_nl v>)  -> per-warp partials of a_k
-//   3  projector scatter U += chi alpha  ||  every warp reduces the a_k partials
+//   3  projector scatter U += chi alpha (atomic only where projector spheres overlap)  ||
+//      every warp reduces the a_k partials
 //   4  w = U - a_k v, P <- w, U <- v  -> per-warp partials of b_k^2
 // After barrier 4 every warp reduces the b partials itself (the same tree in every warp, so
 // every thread sees the same b_k and takes the same branch).  a_k and b_k^2 are summed per
@@ -148,8 +150,10 @@ __global__ void __launch_bounds__(MAXT, 1)
   float2 *red_a = reinterpret_cast<float2 *>(sab + 128);  // per-warp double-float partials
   float2 *red_b = red_a + kMaxWarps;
   cur += sizeof(double) * (2 * kMaxWarps + 128);
-  float *cacc = reinterpret_cast<float *>(cur);
-  cur += sizeof(float) * maxi * NLM;
+  // gathered c per (warp, image): warp w's range covers images k_first(w).. so k + w is
+  // unique for every pair it visits; plain stores, summed per slot in a fixed order
+  float *part = reinterpret_cast<float *>(cur);
+  cur += sizeof(float) * (maxi + kMaxWarps) * NLM;
   float *alpha = reinterpret_cast<float *>(cur);
   cur += sizeof(float) * maxi * NLM;
   int *img = reinterpret_cast<int *>(cur);
@@ -160,7 +164,8 @@ __global__ void __launch_bounds__(MAXT, 1)
   int *pref = bext + maxi;      // maxi + 1
   int *kept = pref + maxi + 1;
   int *koff = kept + maxi;      // maxi + 1
-  int *cnt = koff + maxi + 1;   // [0] images, [1] slots, [2] overflow
+  int *slot_first = koff + maxi + 1;  // first image of every slot (images sorted by atom)
+  int *cnt = slot_first + maxi;  // [0] images, [1] slots, [2] overflow
 
   typename Rec::vec_t *rec = reinterpret_cast<typename Rec::vec_t *>(
       proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
@@ -246,7 +251,10 @@ __global__ void __launch_bounds__(MAXT, 1)
         }
         if (k < n) {
           slot[k] = g;
-          if (start) slot_type[g] = type;
+          if (start) {
+            slot_type[g] = type;
+            slot_first[g] = k;
+          }
           blo[k] = lo;
           bext[k] = ext;
           pref[k] = offset + incl - npts;
@@ -265,7 +273,6 @@ __global__ void __launch_bounds__(MAXT, 1)
         P4[e] = zero4;
         U4[e] = zero4;
       }
-      for (int e = threadIdx.x - 32; e < maxi * NLM; e += blockDim.x - 32) cacc[e] = 0.f;
     }
     __syncthreads();
     const int n_img = cnt[0], n_slot = cnt[1];
@@ -322,6 +329,22 @@ __global__ void __launch_bounds__(MAXT, 1)
       if (lane == 0) kept[kk] = kept_n;
     }
     __syncthreads();
+    // Points that more than one list entry meets (where projector spheres of different images
+    // overlap) get bit 31 of their index: the scatter adds there atomically, everywhere else
+    // with a plain add.  U, still zero, counts the entries per point.
+    {
+      int *cov = reinterpret_cast<int *>(U);
+      for (int kk = warp; kk < n_img; kk += nw)
+        for (int i = lane; i < kept[kk]; i += 32) atomicAdd(&cov[ridx[pref[kk] + i]], 1);
+      __syncthreads();
+      for (int kk = warp; kk < n_img; kk += nw)
+        for (int i = lane; i < kept[kk]; i += 32) {
+          const unsigned e = ridx[pref[kk] + i];
+          if (cov[e] > 1) ridx[pref[kk] + i] = e | 0x80000000u;
+        }
+      __syncthreads();
+      for (int e = threadIdx.x; e < (nc >> 2); e += blockDim.x) U4[e] = zero4;
+    }
     if (warp == 0) {  // exclusive scan of kept -> koff
       int offset = 0;
       for (int base = 0; base < n_img; base += 32) {
@@ -385,16 +408,15 @@ __global__ void __launch_bounds__(MAXT, 1)
             }
 #pragma unroll
             for (int u = 0; u < kStream; u++) {
-              const float val = (i0 + 32 * u < kend) ? P[ix[u]] : 0.f;
+              const float val = (i0 + 32 * u < kend) ? P[ix[u] & 0x7fffffffu] : 0.f;
 #pragma unroll
               for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][s], val, acc[s]);
             }
           }
-          const int sl = slot[k];
 #pragma unroll
           for (int s = 0; s < NLM; s++) {
             const float r = lk::warp_sum(acc[s]);
-            if (lane == 0) atomicAdd(&cacc[sl * NLM + s], r);
+            if (lane == 0) part[(k + warp) * NLM + s] = r;
           }
           pos = kend;
           k++;
@@ -513,8 +535,15 @@ __global__ void __launch_bounds__(MAXT, 1)
         const int sl = e / NLM, r = e - sl * NLM;
         const TypeDesc &td = p.types[slot_type[sl]];
         const int l = p.rank_l[r];
-        const float cv = cacc[e] * inv;
-        cacc[e] = 0.f;
+        // c of the slot: its images' partials from every warp whose range meets them, in a
+        // fixed order (no atomics: shared-memory float atomics on a few hot addresses stall)
+        float csum = 0.f;
+        for (int k = slot_first[sl]; k < n_img && slot[k] == sl; k++) {
+          if (koff[k + 1] == koff[k]) continue;
+          const int w1 = (koff[k + 1] - 1) / per;
+          for (int w = koff[k] / per; w <= w1; w++) csum += part[(k + w) * NLM + r];
+        }
+        const float cv = csum * inv;
         const float gl = (td.chan_mask & (1 << l)) ? float(td.gamma[l]) : 0.f;
         const float al = gl * cv;
         alpha[e] = al;
@@ -550,7 +579,10 @@ __global__ void __launch_bounds__(MAXT, 1)
               float val = 0.f;
 #pragma unroll
               for (int s = 0; s < NLM; s++) val = fmaf(c[u][s], coef[s], val);
-              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u]], val);
+              if (i0 + 32 * u < kend) {
+                if (ix[u] & 0x80000000u) atomicAdd(&U[ix[u] & 0x7fffffffu], val);
+                else U[ix[u]] += val;  // the point's only entry: no other writer
+              }
             }
           }
           pos = kend;

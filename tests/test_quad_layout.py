@@ -210,3 +210,60 @@ def test_split_passes_equal_the_direct_stencil(n, tile):
     want = _stencil_direct(v, np.concatenate([[0.0], c[1:]])) + dv * v
     np.testing.assert_allclose(U[:, :, :n], want, rtol=1e-12, atol=1e-12)
     assert np.all(U[:, :, n:] == 0.0)
+
+
+def _gather_pairs(kept, nw):
+    """The (image, warp) pairs the kernel's gather loop writes (part[k + w]) and the ones the
+    alpha phase reads, restated from lanczos_quad.cuh."""
+    n_img = len(kept)
+    koff = np.concatenate([[0], np.cumsum(kept)])
+    total = int(koff[-1])
+    per = (total + nw - 1) // nw
+    written = set()
+    for w in range(nw):
+        r_begin = min(total, w * per)
+        r_end = min(total, r_begin + per)
+        lo, hi = 0, n_img  # largest k with koff[k] <= r_begin
+        while lo < hi:
+            mid = (lo + hi + 1) >> 1
+            if koff[mid] <= r_begin:
+                lo = mid
+            else:
+                hi = mid - 1
+        k = min(lo, max(n_img - 1, 0))
+        pos = r_begin
+        while pos < r_end:
+            kend = min(r_end, koff[k + 1])
+            written.add((k, w))
+            pos = kend
+            k += 1
+    read = set()
+    for k in range(n_img):
+        if koff[k + 1] == koff[k]:
+            continue
+        for w in range(koff[k] // per, (koff[k + 1] - 1) // per + 1):
+            read.add((k, w))
+    return written, read, koff, per
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_gather_partials_cover_every_point_once(seed):
+    """Every point of the node's list is summed exactly once into its image's c: the warps'
+    ranges tile [0, total), every (image, warp) pair the alpha phase reads was written by that
+    warp in the same step, and the partial index k + w never collides or leaves the array."""
+    rng = np.random.default_rng(seed)
+    n_img = int(rng.integers(1, 120))
+    nw = int(rng.integers(2, 17))
+    kept = rng.integers(0, 900, n_img) * (rng.random(n_img) > 0.15)
+    written, read, koff, per = _gather_pairs(kept, nw)
+    assert read <= written
+    idx = [k + w for (k, w) in written]
+    assert len(set(idx)) == len(idx) and max(idx, default=0) < n_img + 32
+    # each point belongs to exactly one warp range and one image: the read pairs cover it once
+    total = int(koff[-1])
+    covered = np.zeros(total, dtype=int)
+    for (k, w) in read:
+        lo = max(koff[k], w * per)
+        hi = min(koff[k + 1], min(total, w * per + per))
+        covered[lo:hi] += 1
+    assert np.all(covered == 1)
