@@ -32,8 +32,7 @@
 //   1  projector gather c = chi^T P (per-warp ranges of the node's list, one partial per
 //      warp and image, no atomics)  ||  pass A
 //   2  pass B  ||  alpha = Gamma c / b (and <v, V_nl v>)  -> per-warp partials of a_k
-//   3  projector scatter U += chi alpha (atomic only where projector spheres overlap)  ||
-//      every warp reduces the a_k partials
+//   3  projector scatter U += chi alpha  ||  every warp reduces the a_k partials
 //   4  w = U - a_k v, P <- w, U <- v  -> per-warp partials of b_k^2
 // After barrier 4 every warp reduces the b partials itself (the same tree in every warp, so
 // every thread sees the same b_k and takes the same branch).  a_k and b_k^2 are summed per
@@ -329,22 +328,6 @@ __global__ void __launch_bounds__(MAXT, 1)
       if (lane == 0) kept[kk] = kept_n;
     }
     __syncthreads();
-    // Points that more than one list entry meets (where projector spheres of different images
-    // overlap) get bit 31 of their index: the scatter adds there atomically, everywhere else
-    // with a plain add.  U, still zero, counts the entries per point.
-    {
-      int *cov = reinterpret_cast<int *>(U);
-      for (int kk = warp; kk < n_img; kk += nw)
-        for (int i = lane; i < kept[kk]; i += 32) atomicAdd(&cov[ridx[pref[kk] + i]], 1);
-      __syncthreads();
-      for (int kk = warp; kk < n_img; kk += nw)
-        for (int i = lane; i < kept[kk]; i += 32) {
-          const unsigned e = ridx[pref[kk] + i];
-          if (cov[e] > 1) ridx[pref[kk] + i] = e | 0x80000000u;
-        }
-      __syncthreads();
-      for (int e = threadIdx.x; e < (nc >> 2); e += blockDim.x) U4[e] = zero4;
-    }
     if (warp == 0) {  // exclusive scan of kept -> koff
       int offset = 0;
       for (int base = 0; base < n_img; base += 32) {
@@ -408,7 +391,7 @@ __global__ void __launch_bounds__(MAXT, 1)
             }
 #pragma unroll
             for (int u = 0; u < kStream; u++) {
-              const float val = (i0 + 32 * u < kend) ? P[ix[u] & 0x7fffffffu] : 0.f;
+              const float val = (i0 + 32 * u < kend) ? P[ix[u]] : 0.f;
 #pragma unroll
               for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][s], val, acc[s]);
             }
@@ -579,10 +562,8 @@ __global__ void __launch_bounds__(MAXT, 1)
               float val = 0.f;
 #pragma unroll
               for (int s = 0; s < NLM; s++) val = fmaf(c[u][s], coef[s], val);
-              if (i0 + 32 * u < kend) {
-                if (ix[u] & 0x80000000u) atomicAdd(&U[ix[u] & 0x7fffffffu], val);
-                else U[ix[u]] += val;  // the point's only entry: no other writer
-              }
+              // fire-and-forget shared atomics: a plain read-add-write waits on the read
+              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u]], val);
             }
           }
           pos = kend;
