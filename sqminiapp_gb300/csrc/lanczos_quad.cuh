@@ -426,6 +426,14 @@ __global__ void __launch_bounds__(MAXT, 1)
         float2 xm2 = make_float2(0.f, 0.f), xp2 = make_float2(0.f, 0.f);
         float4 xm1 = zero4, xp1 = zero4;
         const float2 *P2c = reinterpret_cast<const float2 *>(P);
+        // U and Veff of plane z+1 load while plane z is computed (in the 12-warp budget; the
+        // 16-warp one has no registers to spare for it)
+        constexpr bool kPrefetch = MAXT <= 384;
+        float4 nuo = zero4, ndv = zero4;
+        if constexpr (kPrefetch) {
+          nuo = U4[row4 + zbA * PS4];
+          ndv = __ldg(vrow + (size_t)zbA * VPS4);
+        }
         for (int z0 = zbA; z0 < zeA; z0 += W) {
 #pragma unroll
           for (int s = 0; s < W; s++) {
@@ -440,7 +448,18 @@ __global__ void __launch_bounds__(MAXT, 1)
             if (hp1) xp1 = P4c[i4 + 1];
             if (hp2) xp2 = P2c[2 * i4 + 4];
             const float4 c = RING(0);
-            const float4 dv = __ldg(vrow + (size_t)z * VPS4);
+            float4 dv, uo;
+            if constexpr (kPrefetch) {
+              dv = ndv;
+              uo = nuo;
+              if (z + 1 < zeA) {
+                nuo = U4[i4 + PS4];
+                ndv = __ldg(vrow + (size_t)(z + 1) * VPS4);
+              }
+            } else {
+              dv = __ldg(vrow + (size_t)z * VPS4);
+              uo = U4[i4];
+            }
             const float2 vs01 = mul2(lo(c), inv2), vs23 = mul2(hi(c), inv2);  // v_k
             float2 h01 = mul2(lo(dv), vs01), h23 = mul2(hi(dv), vs23);
 #pragma unroll
@@ -466,7 +485,6 @@ __global__ void __launch_bounds__(MAXT, 1)
             h01.y = in1 ? h01.y : 0.f;
             h23.x = in2 ? h23.x : 0.f;
             h23.y = in3 ? h23.y : 0.f;
-            const float4 uo = U4[i4];
             const float2 n01 = fma2(ntb2, lo(uo), h01), n23 = fma2(ntb2, hi(uo), h23);
             U4[i4] = make_float4(n01.x, n01.y, n23.x, n23.y);
             const float2 pa = fma2(vs01, h01, mul2(vs23, h23));
@@ -482,20 +500,24 @@ __global__ void __launch_bounds__(MAXT, 1)
 #pragma unroll
         for (int d = 1; d <= O; d++) cys[d] = splat((ISO ? p.czf[d] : p.cyf[d]) * inv);
         const int pl4 = zB * PS4 + ql;  // quad index of (x0, y = 0) in plane zB
+        // ring[j] holds row ybB - 6 + j; row y+7 and U of row y+1 load while row y computes
         float4 ring[W];
 #pragma unroll
-        for (int q = -O; q < O; q++) {
-          const int yq = ybB + q;
-          ring[q + O + 1] = (yq >= 0 && yq < ny) ? P4c[pl4 + yq * nq] : zero4;
+        for (int j = 0; j < W; j++) {
+          const int yq = ybB - O + j;
+          ring[j] = (yq >= 0 && yq < ny) ? P4c[pl4 + yq * nq] : zero4;
         }
+        float4 nuo = U4[pl4 + ybB * nq];
         for (int y0 = ybB; y0 < yeB; y0 += W) {
 #pragma unroll
           for (int s = 0; s < W; s++) {
             const int y = y0 + s;
             if (y >= yeB) break;
-            const int qn = y + O;
-            ring[s] = qn < ny ? P4c[pl4 + qn * nq] : zero4;
-#define RING(dd) ring[(s + (dd) + O + 1) % W]
+            const int u4 = pl4 + y * nq;
+            const float4 uo = nuo;
+            const float4 nring = y + O + 1 < ny ? P4c[u4 + (O + 1) * nq] : zero4;
+            if (y + 1 < yeB) nuo = U4[u4 + nq];
+#define RING(dd) ring[(s + (dd) + O) % W]
             float2 h01 = make_float2(0.f, 0.f), h23 = make_float2(0.f, 0.f);
 #pragma unroll
             for (int d = 1; d <= O; d++) {
@@ -504,12 +526,11 @@ __global__ void __launch_bounds__(MAXT, 1)
             }
             const float4 c = RING(0);
 #undef RING
-            const int u4 = pl4 + y * nq;
-            const float4 uo = U4[u4];
             const float2 n01 = add2(lo(uo), h01), n23 = add2(hi(uo), h23);
             U4[u4] = make_float4(n01.x, n01.y, n23.x, n23.y);
             const float2 pa = fma2(mul2(lo(c), inv2), h01, mul2(mul2(hi(c), inv2), h23));
             ka.add(pa.x + pa.y);
+            ring[s] = nring;  // row y-6 leaves, row y+7 joins
           }
         }
       }
@@ -577,8 +598,18 @@ __global__ void __launch_bounds__(MAXT, 1)
       {
         const float2 na2 = splat(-(adf.hi + adf.lo));
         Kahan kb;
+        // the next quad's P and U are read before this quad's are written
+        float4 npv = zero4, nuv = zero4;
+        if (threadIdx.x < (nc >> 2)) {
+          npv = P4[threadIdx.x];
+          nuv = U4[threadIdx.x];
+        }
         for (int e = threadIdx.x; e < (nc >> 2); e += blockDim.x) {
-          const float4 pv = P4[e], uv = U4[e];
+          const float4 pv = npv, uv = nuv;
+          if (e + (int)blockDim.x < (nc >> 2)) {
+            npv = P4[e + blockDim.x];
+            nuv = U4[e + blockDim.x];
+          }
           const float2 v01 = mul2(lo(pv), inv2), v23 = mul2(hi(pv), inv2);
           const float2 w01 = fma2(na2, v01, lo(uv)), w23 = fma2(na2, v23, hi(uv));
           P4[e] = make_float4(w01.x, w01.y, w23.x, w23.y);
