@@ -12,7 +12,7 @@ int lanczos_quad_threads(const LanczosParams &p) {
 }
 
 size_t lanczos_quad_smem_bytes(const LanczosParams &p) {
-  const size_t nc = (size_t)p.nz * p.ny * p.pitch;
+  const size_t nc = (size_t)p.nz * lq::quad_plane_floats(p.ny, p.pitch);
   const int nlm = mask_nlm(kernel_mask(p.union_mask));
   size_t b = sizeof(float) * 2 * nc;                          // P, U
   b += sizeof(double) * (2 * lk::kMaxWarps + 128);           // a_k / b_k partials, a[], b[]

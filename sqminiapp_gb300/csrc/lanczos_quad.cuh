@@ -5,12 +5,12 @@
 // + the Kleinman-Bylander projectors of the atom images that meet the cube,
 // src/lsdft_matvec.cc:25-149); FP32 vectors, corrected operator, full projector records.
 //
-// Layout.  P and U are both [nz][ny][pitch] floats in shared memory, pitch = 4*ceil(nx/4):
-// every row starts on a 16-byte boundary and holds whole float4 quads; the pad columns
-// [nx, pitch) stay zero.  There are no zero rows or columns between rows: neighbours outside
+// Layout.  P and U are both [nz][ny][pitch] floats in shared memory, pitch = 4*ceil(nx/4),
+// planes padded to a bank-friendly stride (quad_plane_floats): every row starts on a 16-byte
+// boundary and holds whole float4 quads; the pad columns [nx, pitch) and plane pads stay zero.  There are no zero rows or columns between rows: neighbours outside
 // the cube are never loaded (x: the quad loads are predicated off at the row ends; y and z:
 // the register rings start and end with zeros).  A point's P and U indices are the same,
-// (z*ny + y)*pitch + x.
+// z*PS + y*pitch + x.
 //
 // Stencil, split by axis so that two of the three axes come from registers:
 //   pass A  a thread owns one quad (x..x+3) of row y over a z-range and walks z with a
@@ -123,6 +123,15 @@ __device__ __forceinline__ DF df_all_reduce(const float2 *red, int nw) {
   return df_warp_sum(DF{r.x, r.y});
 }
 
+// Floats per z-plane of P and U: ny rows of pitch, plus a pad that makes the plane stride
+// congruent to one row (4 * pitch/4 floats) modulo the 32 banks.  The y pass has nq = pitch/4
+// consecutive threads per plane and consecutive planes on consecutive thread groups, so its
+// float4 accesses then fall on consecutive banks across the whole warp (without the pad two
+// planes of a quarter-warp can share banks, e.g. 27 rows of 28 floats: offset 20 banks).
+__host__ __device__ constexpr int quad_plane_floats(int ny, int pitch) {
+  return ny * pitch + ((pitch - ny * pitch) % 32 + 32) % 32;
+}
+
 template <int MASK, int MAXT, bool ISO>
 __global__ void __launch_bounds__(MAXT, 1)
     lanczos_quad_kernel(const __grid_constant__ LanczosParams p, const float *__restrict__ veffq,
@@ -136,8 +145,8 @@ __global__ void __launch_bounds__(MAXT, 1)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
   const int nq = pitch >> 2;        // quads per row
-  const int PS = ny * pitch;        // plane stride (floats)
-  const int PS4 = ny * nq;          // plane stride (quads)
+  const int PS = quad_plane_floats(ny, pitch);  // plane stride (floats)
+  const int PS4 = PS >> 2;                       // plane stride (quads)
   const int nc = nz * PS;           // floats of P (and of U)
   const int maxi = p.max_img;
 
@@ -282,7 +291,7 @@ __global__ void __launch_bounds__(MAXT, 1)
       __syncthreads();
       continue;
     }
-    if (threadIdx.x == 0) P[((nz - 1) / 2 * ny + (ny - 1) / 2) * pitch + (nx - 1) / 2] = 1.f;
+    if (threadIdx.x == 0) P[(nz - 1) / 2 * PS + (ny - 1) / 2 * pitch + (nx - 1) / 2] = 1.f;
 
     // ---- this node's projector list: one warp per image, support points only ----
     for (int kk = warp; kk < n_img; kk += nw) {

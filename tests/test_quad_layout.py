@@ -19,6 +19,12 @@ O = 6
 MAX_THREADS = 512
 
 
+def plane_floats(n, pitch):
+    """Floats per z-plane: n rows of pitch plus the pad that makes the stride one row modulo
+    the 32 banks (quad_plane_floats in lanczos_quad.cuh)."""
+    return n * pitch + ((pitch - n * pitch) % 32 + 32) % 32
+
+
 def quad_threads(n, tile):
     nq = (n + 3) // 4
     return max(64, 32 * ((nq * n * tile + 31) // 32))
@@ -79,12 +85,14 @@ def test_passes_cover_every_quad_once(n, tile):
 def test_shared_reads_stay_in_the_row(n, tile):
     nq, ql, (yA, zb, ze, actA), _ = thread_maps(n, tile)
     pitch = 4 * nq
-    nc = n * n * pitch
+    ps = plane_floats(n, pitch)
+    assert ps % 4 == 0 and ps >= n * pitch
+    nc = n * ps
     for i in np.nonzero(actA)[0]:
         q = ql[i]
         for z in range(zb[i], ze[i]):
-            row0 = (z * n + yA[i]) * pitch  # first float of the row
-            i4 = (z * n + yA[i]) * nq + q
+            row0 = z * ps + yA[i] * pitch  # first float of the row
+            i4 = (z * ps + yA[i] * pitch) // 4 + q
             reads = []
             if q >= 2:  # float2 at x0-6
                 reads += [2 * (2 * i4 - 3), 2 * (2 * i4 - 3) + 1]
@@ -267,3 +275,32 @@ def test_gather_partials_cover_every_point_once(seed):
         hi = min(koff[k + 1], min(total, w * per + per))
         covered[lo:hi] += 1
     assert np.all(covered == 1)
+
+
+@pytest.mark.parametrize("n,tile", CASES)
+def test_float4_accesses_are_bank_conflict_free(n, tile):
+    """Every warp-wide float4 access of the z pass (a row of quads per thread group) and of the
+    y pass (a plane per thread group, at one ring row) is served in the minimum four
+    wavefronts: within each quarter-warp whose threads work on the same z- (y-) range, the
+    eight 16-byte accesses use distinct banks.  (A quarter-warp that straddles two ranges
+    reads planes (rows) a range length apart and may pay one extra wavefront.)"""
+    nq, ql, (yA, zb, ze, actA), (zB, yb, ye, actB) = thread_maps(n, tile)
+    pitch = 4 * nq
+    ps = plane_floats(n, pitch)
+    nt = len(ql)
+
+    def check(word, active, rng):
+        checked = 0
+        for q0 in range(0, nt, 8):
+            ts = [t for t in range(q0, min(q0 + 8, nt)) if active[t]]
+            if len({int(rng[t]) for t in ts}) != 1:
+                continue
+            banks = [(int(word[t]) + j) % 32 for t in ts for j in range(4)]
+            assert len(banks) == len(set(banks)), (n, tile, q0)
+            checked += 1
+        assert checked >= (np.count_nonzero(active) // 8) * 3 // 4
+
+    # z pass, every thread at the same offset into its z-range (all offsets alike)
+    check(zb * ps + yA * pitch + 4 * ql, actA, zb)
+    # y pass, every thread at the same offset into its y-range
+    check(zB * ps + yb * pitch + 4 * ql, actB, yb)
