@@ -144,6 +144,16 @@ sq_status sq_nodes_and_weights_device(sq_handle *h, const double *d_veff, double
  * (capacity overflow, Lanczos breakdown, QL non-convergence, device timeout). */
 sq_status sq_sync_status(sq_handle *h, void *stream);
 
+/* Gauss quadrature of given tridiagonals: implicit QL on a[i][0..n_qp) (diagonal) and
+ * b[i][0..n_qp-1) (sub-diagonal; b[i][n_qp-1] is ignored, as the reference zeroes it), giving
+ * lambda, weights [n_nodes][n_qp] and lambda_min / lambda_max [n_nodes].  HOST buffers; runs
+ * on `device`.  Replaces TridiagEigenVecSolve_NodesAndWeights (src/lsdft.h:163-164,
+ * src/lsdft_tools.cc:912-1026), which exit(1)s after 50 sweeps (:950-952); here every node's
+ * outputs are written and SQ_NO_CONVERGENCE is returned if any node needed more. */
+sq_status sq_tridiag_nodes_and_weights(const double *a, const double *b, long n_nodes, int n_qp,
+                                       double *lambda, double *weights, double *lambda_min,
+                                       double *lambda_max, int device);
+
 /* Copy the Lanczos coefficients a_k, b_k (k < n_qp) of the last nodes_and_weights call to
  * host arrays [n][n_qp] (the lssgq recurrence of src/lsdft_scf.cc:111-150). */
 sq_status sq_copy_lanczos_coefficients(sq_handle *h, double *a, double *b, long n);
@@ -193,6 +203,13 @@ sq_status sq_batch_nodes_and_weights(sq_handle *const *cells, int n_cells,
 /* Device time (ms) of the kernels of the last nodes_and_weights call, measured with CUDA
  * events on the stream they ran on: ms[0] Lanczos kernel, ms[1] quadrature kernel. */
 sq_status sq_last_kernel_times(sq_handle *h, double *ms);
+
+/* Fault-injection self-test of the bounded device-side waits (no counterpart in the reference,
+ * which has no device code): runs the Fermi-level kernel on a small synthetic input with one
+ * CTA leaving before the first grid barrier and a short poll limit.  The other CTAs give up
+ * after about 0.4 ms of polling and return, so the call returns SQ_DEVICE_TIMEOUT and the
+ * context stays usable; SQ_OK would mean the wait did not report its timeout. */
+sq_status sq_fermi_timeout_selftest(int device);
 
 /* Measure the FP32 FMA throughput of the device (TFLOP/s) with a register-resident FMA
  * chain on every SM; the peak against which the FP32 Lanczos kernel is reported. */

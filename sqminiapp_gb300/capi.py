@@ -82,6 +82,9 @@ SIGNATURES = {
     "sq_fermi_density_energy_noalloc": (ctypes.c_int, [_vp, _vp, _l, ctypes.c_int, _d, _d, _d,
                                                        _d, ctypes.c_int, _vp, _dp, _vp]),
     "sq_measure_fp32_peak": (ctypes.c_int, [ctypes.c_int, _dp]),
+    "sq_tridiag_nodes_and_weights": (ctypes.c_int, [_dp, _dp, _l, ctypes.c_int, _dp, _dp, _dp,
+                                                    _dp, ctypes.c_int]),
+    "sq_fermi_timeout_selftest": (ctypes.c_int, [ctypes.c_int]),
     "sq_scf_begin": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _dp]),
     "sq_scf_begin_device": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _vp]),
     "sq_scf_step": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfResult)]),

@@ -452,11 +452,14 @@ sq_status device_status(sq_handle *h, cudaStream_t s) {
   int st = 0;
   ck(cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, s), "status D2H");
   ck(cudaStreamSynchronize(s), "sync");
+  // the upstream cause first: a Lanczos breakdown (b_k zero or not finite) also leaves a
+  // tridiagonal that QL may not converge on
   if (st & sq::kStatusTimeout) return fail(SQ_DEVICE_TIMEOUT, "a device-side wait gave up");
   if (st & sq::kStatusCapacity) return fail(SQ_CAPACITY, "per-node image list overflow");
+  if (st & sq::kStatusBreakdown)
+    return fail(SQ_LANCZOS_BREAKDOWN, "Lanczos breakdown (b_k zero or not finite)");
   if (st & sq::kStatusNoConvergence)
     return fail(SQ_NO_CONVERGENCE, "Too many iterations in Tridiagonal solver");
-  if (st & sq::kStatusBreakdown) return fail(SQ_LANCZOS_BREAKDOWN, "Lanczos breakdown (b_k == 0)");
   return SQ_OK;
 }
 
@@ -885,6 +888,70 @@ sq_status sq_batch_nodes_and_weights(sq_handle *const *cells, int n_cells, const
       st = device_status(cells[c], cells[c]->own_stream);
       if (st != SQ_OK) return st;
     }
+    return SQ_OK;
+  });
+}
+
+sq_status sq_tridiag_nodes_and_weights(const double *a, const double *b, long n_nodes, int n_qp,
+                                       double *lambda, double *weights, double *lambda_min,
+                                       double *lambda_max, int device) {
+  if (!a || !b || !lambda || !weights || !lambda_min || !lambda_max)
+    return fail(SQ_BAD_INPUT, "null argument");
+  if (n_nodes <= 0 || n_qp <= 0 || n_qp > 64)
+    return fail(SQ_BAD_INPUT, "n_nodes must be positive and n_qp in 1..64");
+  return guarded([&] {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    const size_t nq = (size_t)n_nodes * n_qp;
+    std::vector<double> ab(2 * nq);  // the kernel's [node][a | b] rows
+    for (long i = 0; i < n_nodes; i++) {
+      std::memcpy(&ab[(size_t)i * 2 * n_qp], a + (size_t)i * n_qp, sizeof(double) * n_qp);
+      std::memcpy(&ab[(size_t)i * 2 * n_qp + n_qp], b + (size_t)i * n_qp, sizeof(double) * n_qp);
+    }
+    sq::DevBuf<double> d_ab(sizeof(double) * ab.size(), "ab");
+    sq::DevBuf<double> d_out(sizeof(double) * (2 * nq + 2 * (size_t)n_nodes), "quadrature");
+    sq::DevBuf<int> d_st(sizeof(int), "status");
+    double *dl = d_out.get(), *dw = dl + nq, *dmin = dw + nq, *dmax = dmin + n_nodes;
+    ck(cudaMemcpy(d_ab.get(), ab.data(), sizeof(double) * ab.size(), cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemset(d_st.get(), 0, sizeof(int)), "status reset");
+    ck(sq::launch_quadrature(d_ab.get(), n_nodes, n_qp, dl, dw, dmin, dmax, d_st.get(), 0),
+       "quadrature");
+    int st = 0;
+    ck(cudaMemcpy(&st, d_st.get(), sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+    ck(cudaMemcpy(lambda, dl, sizeof(double) * nq, cudaMemcpyDeviceToHost), "D2H");
+    ck(cudaMemcpy(weights, dw, sizeof(double) * nq, cudaMemcpyDeviceToHost), "D2H");
+    ck(cudaMemcpy(lambda_min, dmin, sizeof(double) * n_nodes, cudaMemcpyDeviceToHost), "D2H");
+    ck(cudaMemcpy(lambda_max, dmax, sizeof(double) * n_nodes, cudaMemcpyDeviceToHost), "D2H");
+    if (st & sq::kStatusNoConvergence)
+      return fail(SQ_NO_CONVERGENCE, "Too many iterations in Tridiagonal solver");
+    return SQ_OK;
+  });
+}
+
+sq_status sq_fermi_timeout_selftest(int device) {
+  return guarded([&] {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    int sms = 0;
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "sm count");
+    const int grid = std::max(2, std::min(sms, 64));
+    const long long n = 4096, nqp = 4;
+    std::vector<double> lam(n * nqp), w(n * nqp, 1.0 / nqp);
+    for (size_t i = 0; i < lam.size(); i++) lam[i] = -1.0 + 2.0 * (double)i / (double)lam.size();
+    sq::DevBuf<double> d_in(sizeof(double) * 2 * lam.size(), "inputs");
+    sq::DevBuf<double> d_scr(sizeof(double) * ((size_t)grid * 16 + 4), "scratch");
+    sq::DevBuf<unsigned> d_bar(sizeof(unsigned) * 2, "barrier");
+    sq::DevBuf<int> d_st(sizeof(int), "status");
+    ck(cudaMemcpy(d_in.get(), lam.data(), sizeof(double) * lam.size(), cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemcpy(d_in.get() + lam.size(), w.data(), sizeof(double) * w.size(),
+                  cudaMemcpyHostToDevice), "H2D");
+    ck(cudaMemset(d_st.get(), 0, sizeof(int)), "status reset");
+    ck(sq::launch_fermi_timeout_selftest(d_in.get(), d_in.get() + lam.size(), n, (int)nqp,
+                                         d_scr.get() + (size_t)grid * 16, d_scr.get(), d_bar.get(),
+                                         d_st.get(), grid, 0),
+       "fermi (timeout self-test)");
+    ck(cudaDeviceSynchronize(), "sync");
+    int st = 0;
+    ck(cudaMemcpy(&st, d_st.get(), sizeof(int), cudaMemcpyDeviceToHost), "D2H");
+    if (st & sq::kStatusTimeout) return fail(SQ_DEVICE_TIMEOUT, "a device-side wait gave up");
     return SQ_OK;
   });
 }

@@ -48,8 +48,9 @@ __device__ double block_sum_d(double v, double *red) {
   return t;  // valid in thread 0
 }
 
-// All CTAs meet here.  Returns false (in every thread of the CTA) if the wait gave up.
-__device__ bool grid_barrier(unsigned *bar, int *status, int *flag_smem) {
+// All CTAs meet here.  Returns false (in every thread of the CTA) if the wait gave up after
+// spin_limit polls.
+__device__ bool grid_barrier(unsigned *bar, int *status, int *flag_smem, long long spin_limit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned *gen_p = bar + 1;
@@ -64,7 +65,7 @@ __device__ bool grid_barrier(unsigned *bar, int *status, int *flag_smem) {
     } else {
       long long spins = 0;
       while (*gen_p == gen) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicOr(status, kStatusTimeout);
           ok = 0;
           break;
@@ -88,8 +89,11 @@ __global__ void __launch_bounds__(kFermiBlock)
                  long long n_nodes, int nqp, double beta, double n_electrons, double dV,
                  double tol, int maxit, double *__restrict__ rho, double *__restrict__ out,
                  double *__restrict__ scratch, unsigned *__restrict__ bar,
-                 int *__restrict__ status) {
+                 int *__restrict__ status, long long spin_limit, int skip_block) {
   __shared__ double red[kFermiBlock / 32];
+  // fault injection of the timeout self-test: one CTA leaves before its first arrival, so
+  // every other CTA's first barrier wait runs out
+  if ((int)blockIdx.x == skip_block) return;
   __shared__ double bcast[2];
   __shared__ int flag;
   const int G = gridDim.x;
@@ -123,7 +127,7 @@ __global__ void __launch_bounds__(kFermiBlock)
     for (int i = 1; i < kFermiBlock / 32; i++) m = fmax(m, red[i]);
     scratch[G + blockIdx.x] = m;
   }
-  if (!grid_barrier(bar, status, &flag)) return;
+  if (!grid_barrier(bar, status, &flag, spin_limit)) return;
   if (threadIdx.x == 0) {
     double a = scratch[0], b = scratch[G];
     for (int i = 1; i < G; i++) {
@@ -145,7 +149,7 @@ __global__ void __launch_bounds__(kFermiBlock)
     for (long long e = tid; e < n; e += stride) c += 2.0 * w[e] * fermi_dirac(beta, lambda[e], mid);
     c = block_sum_d(c, red);
     if (threadIdx.x == 0) scratch[(2 + it) * (long long)G + blockIdx.x] = c;
-    if (!grid_barrier(bar, status, &flag)) return;
+    if (!grid_barrier(bar, status, &flag, spin_limit)) return;
     if (threadIdx.x == 0) {
       double ne = 0.0;
       for (int i = 0; i < G; i++) ne += scratch[(2 + it) * (long long)G + i];
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(kFermiBlock)
     scratch[rowE + blockIdx.x] = eb;
     scratch[rowS + blockIdx.x] = ent;
   }
-  if (!grid_barrier(bar, status, &flag)) return;
+  if (!grid_barrier(bar, status, &flag, spin_limit)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     double E = 0.0, S = 0.0;
     for (int i = 0; i < G; i++) {
@@ -244,18 +248,41 @@ void set_noalloc_error(const std::string &msg);
 
 size_t fermi_scratch_doubles(int grid, int maxit) { return (size_t)grid * (maxit + 4); }
 
-cudaError_t launch_fermi(const double *lambda, const double *w, long long n_nodes, int nqp,
-                         double beta, double n_electrons, double dV, double tol, int maxit,
-                         double *rho, double *out, double *scratch, unsigned *barrier,
-                         int *status, int grid, cudaStream_t s) {
+namespace {
+cudaError_t launch_fermi_impl(const double *lambda, const double *w, long long n_nodes, int nqp,
+                              double beta, double n_electrons, double dV, double tol, int maxit,
+                              double *rho, double *out, double *scratch, unsigned *barrier,
+                              int *status, int grid, cudaStream_t s, long long spin_limit,
+                              int skip_block) {
   cudaError_t e = cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
   void *args[] = {(void *)&lambda, (void *)&w,   (void *)&n_nodes, (void *)&nqp,
                   (void *)&beta,   (void *)&n_electrons, (void *)&dV, (void *)&tol,
                   (void *)&maxit,  (void *)&rho, (void *)&out,     (void *)&scratch,
-                  (void *)&barrier, (void *)&status};
+                  (void *)&barrier, (void *)&status, (void *)&spin_limit, (void *)&skip_block};
   return cudaLaunchCooperativeKernel((const void *)fermi_kernel, dim3(grid), dim3(kFermiBlock),
                                      args, 0, s);
+}
+}  // namespace
+
+cudaError_t launch_fermi(const double *lambda, const double *w, long long n_nodes, int nqp,
+                         double beta, double n_electrons, double dV, double tol, int maxit,
+                         double *rho, double *out, double *scratch, unsigned *barrier,
+                         int *status, int grid, cudaStream_t s) {
+  return launch_fermi_impl(lambda, w, n_nodes, nqp, beta, n_electrons, dV, tol, maxit, rho, out,
+                           scratch, barrier, status, grid, s, kSpinLimit, -1);
+}
+
+// Fault-injection self-test of the grid barrier's bounded wait: the same cooperative launch
+// with one CTA leaving before its first arrival and a short poll limit (about 4096 polls of
+// 100 ns), so the other CTAs give up, record kStatusTimeout and return.  Nothing faults or
+// hangs: the kernel ends and the context stays usable.
+cudaError_t launch_fermi_timeout_selftest(const double *lambda, const double *w, long long n_nodes,
+                                          int nqp, double *out, double *scratch,
+                                          unsigned *barrier, int *status, int grid,
+                                          cudaStream_t s) {
+  return launch_fermi_impl(lambda, w, n_nodes, nqp, 30.0, 1.0, 1.0, 1e-12, 10, nullptr, out,
+                           scratch, barrier, status, grid, s, 1LL << 12, 0);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -70,6 +70,13 @@ cudaError_t launch_fermi(const double *lambda, const double *w, long long n_node
                          double *rho, double *out, double *scratch, unsigned *barrier,
                          int *status, int grid, cudaStream_t s);
 
+// The Fermi kernel with one CTA leaving before the first grid barrier and a short poll limit:
+// the bounded wait of every other CTA runs out (kStatusTimeout); see fermi.cu.
+cudaError_t launch_fermi_timeout_selftest(const double *lambda, const double *w, long long n_nodes,
+                                          int nqp, double *out, double *scratch,
+                                          unsigned *barrier, int *status, int grid,
+                                          cudaStream_t s);
+
 // N_e(lf) = 2 sum w f(lambda - lf) over n_nodes*nqp entries; `partial` holds `grid` doubles.
 cudaError_t launch_electron_count(const double *lambda, const double *w, long long n_nodes,
                                   int nqp, double beta, double lf, double *partial, int grid,
