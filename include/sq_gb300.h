@@ -97,6 +97,55 @@ typedef struct sq_info {
   int kernel_smem_bytes;
 } sq_info;
 
+/* One pseudopotential type in memory, in the units the reference holds after
+ * Read_Pseudopotential (PSD_OBJ, src/ilsdft.h:63-80; src/lsdft_readfiles.cc:858-1101): a radial
+ * grid whose first point is r = 0, V_l in Ha (the file's r V_l in Ry divided by 2r), U_l the
+ * file's u_l / r, the valence density already divided by 4 pi r^2, every array [n_r]. */
+typedef struct sq_psd_desc {
+  int n_r;                  /* radial points, r[0] = 0 (PSD_OBJ.size) */
+  const double *r;          /* RadialGrid */
+  int lmax;                 /* highest l with a potential (PSD_OBJ.lmax, 0..3) */
+  int lloc;                 /* PSEUDOPOTENTIAL_LOCAL: the l whose V_l is the local part */
+  int valence;              /* valence electrons per atom (.ion) */
+  const double *V[4];       /* V_l, l <= lmax (PSD_OBJ.V) */
+  const double *U[4];       /* U_l, l <= lmax and l != lloc (PSD_OBJ.U); NULL otherwise */
+  double rc[4];             /* cutoff radius of U_l (PSD_OBJ.rc) */
+  const double *rho_atom;   /* isolated-atom valence density (PSD_OBJ.uu); NULL = zero */
+} sq_psd_desc;
+
+/* A whole cell in memory: the fields of the reference's LSDFT_OBJ (src/ilsdft.h:85-458) that
+ * its input readers fill (src/lsdft_readfiles.cc:21-789), with the same meanings as the deck
+ * keywords.  Zero SCF fields take the reference's defaults (readfiles.cc:62-102). */
+typedef struct sq_system_desc {
+  int fd_order;             /* FD_ORDER (even, 12 for the reference's stencil) */
+  int bc;                   /* BOUNDARY_CONDITION 1..4 */
+  double cell_half[3];      /* CELL: half side lengths R (bohr) */
+  int grid[3];              /* FD_GRID */
+  double beta;              /* BETA (1/Ha) */
+  double rcut;              /* RADIUS_TRUNC (bohr) */
+  int n_qp;                 /* LANCZOS_DEGREE, 1..64 */
+  int n_types;              /* NTYPE, 1..8 */
+  const sq_psd_desc *psd;   /* [n_types] */
+  int n_atoms;
+  const int *atom_type;     /* [n_atoms], 0..n_types-1 */
+  const double *atom_xyz;   /* [n_atoms][3], centred coordinates in [-R, R) (bohr) */
+  double mixing_parameter;  /* MIXING_PARAMETER (0: 0.3) */
+  int mixing_history;       /* MIXING_HISTORY (0: 7) */
+  int pulay_frequency;      /* PULAY_FREQUENCY (0: 1) */
+  double tol_scf;           /* TOL_SCF (0: 1e-6) */
+  int maxit_scf;            /* MAXIT_SCF (0: 100) */
+  double reference_cutoff;  /* REFERENCE_CUTOFF (0: 0.5) */
+} sq_system_desc;
+
+/* Build the engine from a cell in memory: the same engine sq_create_from_deck builds from the
+ * deck files holding these values.  Every array is copied; the caller may free them after the
+ * call.  Replaces Initialize's readers for a caller that already holds an initialized
+ * LSDFT_OBJ (src/main.cc:21-33, src/lsdft_initObjs.cc:36-93). */
+sq_status sq_create(const sq_system_desc *sys, const sq_options *opt, sq_handle **out);
+/* Host-only setup report of an in-memory cell, as sq_describe_deck for a deck. */
+sq_status sq_describe_system(const sq_system_desc *sys, int faithful, sq_info *info,
+                             double *gamma, double *cutoff);
+
 /* Read <deck_dir>/<name>.inpt/.ion/.relax and <deck_dir>/pseudopotential/<psd> and build the
  * engine.  Replaces Get_Input + Initialize + GetInfluencingAtoms_Nonlocal +
  * CalculateNonlocalProjectors + NonlocalProjectors (src/main.cc:32-44,

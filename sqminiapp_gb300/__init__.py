@@ -57,13 +57,22 @@ class LSDFT:
     """
 
     def __init__(self, deck_dir, name, faithful=False, precision=32, device=0, list_format=0,
-                 kernel=0, tile=0):
+                 kernel=0, tile=0, system=None):
+        """deck_dir/name: the reference's input deck; or deck_dir=name=None and system=a cell
+        in memory (sqminiapp_gb300.system.read_system's dict), built with sq_create."""
         self._lib = lib()
         self._h = ctypes.c_void_p()
         opt = SqOptions(int(bool(faithful)), int(precision), int(device), int(list_format),
                         int(kernel), int(tile))
-        check(self._lib.sq_create_from_deck(deck_dir.encode(), name.encode(), ctypes.byref(opt),
-                                            ctypes.byref(self._h)), "sq_create_from_deck")
+        if system is not None:
+            from .system import to_desc
+            packed = to_desc(system)
+            check(self._lib.sq_create(ctypes.byref(packed.desc), ctypes.byref(opt),
+                                      ctypes.byref(self._h)), "sq_create")
+        else:
+            check(self._lib.sq_create_from_deck(deck_dir.encode(), name.encode(),
+                                                ctypes.byref(opt), ctypes.byref(self._h)),
+                  "sq_create_from_deck")
         info = SqInfo()
         check(self._lib.sq_get_info(self._h, ctypes.byref(info)), "sq_get_info")
         self.info = info

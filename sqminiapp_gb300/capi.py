@@ -43,6 +43,23 @@ class SqInfo(ctypes.Structure):
                 ("kernel_smem_bytes", ctypes.c_int)]
 
 
+class SqPsdDesc(ctypes.Structure):
+    _fields_ = [("n_r", ctypes.c_int), ("r", _dp), ("lmax", ctypes.c_int), ("lloc", ctypes.c_int),
+                ("valence", ctypes.c_int), ("V", _dp * 4), ("U", _dp * 4),
+                ("rc", ctypes.c_double * 4), ("rho_atom", _dp)]
+
+
+class SqSystemDesc(ctypes.Structure):
+    _fields_ = [("fd_order", ctypes.c_int), ("bc", ctypes.c_int),
+                ("cell_half", ctypes.c_double * 3), ("grid", ctypes.c_int * 3),
+                ("beta", ctypes.c_double), ("rcut", ctypes.c_double), ("n_qp", ctypes.c_int),
+                ("n_types", ctypes.c_int), ("psd", ctypes.POINTER(SqPsdDesc)),
+                ("n_atoms", ctypes.c_int), ("atom_type", _ip), ("atom_xyz", _dp),
+                ("mixing_parameter", ctypes.c_double), ("mixing_history", ctypes.c_int),
+                ("pulay_frequency", ctypes.c_int), ("tol_scf", ctypes.c_double),
+                ("maxit_scf", ctypes.c_int), ("reference_cutoff", ctypes.c_double)]
+
+
 class SqScfOptions(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("maxit", ctypes.c_int),
                 ("mixing_parameter", ctypes.c_double), ("mixing_history", ctypes.c_int),
@@ -64,6 +81,10 @@ SIGNATURES = {
     "sq_create_from_deck": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p,
                                            ctypes.POINTER(SqOptions), ctypes.POINTER(_vp)]),
     "sq_destroy": (None, [_vp]),
+    "sq_create": (ctypes.c_int, [ctypes.POINTER(SqSystemDesc), ctypes.POINTER(SqOptions),
+                                 ctypes.POINTER(_vp)]),
+    "sq_describe_system": (ctypes.c_int, [ctypes.POINTER(SqSystemDesc), ctypes.c_int,
+                                          ctypes.POINTER(SqInfo), _dp, _dp]),
     "sq_describe_deck": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
                                         ctypes.POINTER(SqInfo), _dp, _dp]),
     "sq_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(SqInfo)]),

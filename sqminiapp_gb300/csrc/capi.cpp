@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -563,20 +564,33 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
 
 }  // namespace sq
 
-extern "C" {
+namespace {
+sq_status describe(const sq::Deck &d, int faithful, sq_info *info, double *gamma, double *cutoff) {
+  sq::Setup s = sq::build_setup(d, faithful != 0);
+  sq_options opt{faithful, 0, 0, 0, 0, 0};
+  *info = sq_info{};
+  fill_info(*info, d, s, max_images_per_node(s, d), opt);
+  for (size_t t = 0; t < s.types.size(); t++) {
+    if (gamma)
+      for (int l = 0; l < 4; l++) gamma[4 * t + l] = s.types[t].gamma[l];
+    if (cutoff)
+      for (int a = 0; a < 3; a++) cutoff[3 * t + a] = s.pseudocharge_cutoff[3 * t + a];
+  }
+  return SQ_OK;
+}
 
-sq_status sq_create_from_deck(const char *deck_dir, const char *name, const sq_options *opt,
-                              sq_handle **out) {
-  if (!out || !deck_dir || !name) return fail(SQ_BAD_INPUT, "null argument");
+// sq_create_from_deck and sq_create share everything after the deck is in memory.
+sq_status create_from(const std::function<sq::Deck()> &deck, const sq_options *opt,
+                      sq_handle **out) {
   *out = nullptr;
   sq_handle *h = new sq_handle();
   sq_status st = guarded([&] {
-    h->opt = opt ? *opt : sq_options{0, 32, 0, 0};
+    h->opt = opt ? *opt : sq_options{0, 32, 0, 0, 0, 0};
     if (h->opt.precision != 32 && h->opt.precision != 64)
       return fail(SQ_BAD_INPUT, "precision must be 32 or 64");
     if (h->opt.list_format < 0 || h->opt.list_format > 2)
       return fail(SQ_BAD_INPUT, "list_format must be 0, 1 or 2");
-    h->deck = sq::read_deck(deck_dir, name);
+    h->deck = deck();
     h->setup = sq::build_setup(h->deck, h->opt.faithful != 0);
     build_engine(h);
     return SQ_OK;
@@ -588,25 +602,37 @@ sq_status sq_create_from_deck(const char *deck_dir, const char *name, const sq_o
   *out = h;
   return SQ_OK;
 }
+}  // namespace
+
+extern "C" {
+
+sq_status sq_create_from_deck(const char *deck_dir, const char *name, const sq_options *opt,
+                              sq_handle **out) {
+  if (!out || !deck_dir || !name) return fail(SQ_BAD_INPUT, "null argument");
+  const std::string dir(deck_dir), nm(name);
+  return create_from([&] { return sq::read_deck(dir, nm); }, opt, out);
+}
 
 void sq_destroy(sq_handle *h) { delete h; }
+
+
+sq_status sq_create(const sq_system_desc *sys, const sq_options *opt, sq_handle **out) {
+  if (!out || !sys) return fail(SQ_BAD_INPUT, "null argument");
+  return create_from([&] { return sq::deck_from_system(*sys); }, opt, out);
+}
+
+sq_status sq_describe_system(const sq_system_desc *sys, int faithful, sq_info *info,
+                             double *gamma, double *cutoff) {
+  if (!sys || !info) return fail(SQ_BAD_INPUT, "null argument");
+  return guarded([&] { return describe(sq::deck_from_system(*sys), faithful, info, gamma, cutoff); });
+}
 
 sq_status sq_describe_deck(const char *deck_dir, const char *name, int faithful, sq_info *info,
                            double *gamma, double *cutoff) {
   if (!deck_dir || !name || !info) return fail(SQ_BAD_INPUT, "null argument");
   return guarded([&] {
     sq::Deck d = sq::read_deck(deck_dir, name);
-    sq::Setup s = sq::build_setup(d, faithful != 0);
-    sq_options opt{faithful, 0, 0, 0};
-    *info = sq_info{};
-    fill_info(*info, d, s, max_images_per_node(s, d), opt);
-    for (size_t t = 0; t < s.types.size(); t++) {
-      if (gamma)
-        for (int l = 0; l < 4; l++) gamma[4 * t + l] = s.types[t].gamma[l];
-      if (cutoff)
-        for (int a = 0; a < 3; a++) cutoff[3 * t + a] = s.pseudocharge_cutoff[3 * t + a];
-    }
-    return SQ_OK;
+    return describe(d, faithful, info, gamma, cutoff);
   });
 }
 

@@ -12,6 +12,7 @@
 #include <sstream>
 #include <stdexcept>
 
+#include "sq_gb300.h"
 #include "sq_internal.hpp"
 
 namespace sq {
@@ -37,6 +38,24 @@ TokenStream tokenize(const std::string &path) {
   std::string s;
   while (f >> s) ts.tok.push_back(s);
   return ts;
+}
+
+// Checks shared by the file readers and the in-memory description.
+void check_deck(const Deck &d, const std::string &where) {
+  for (int a = 0; a < 3; a++)
+    if (d.grid[a] < 2 || !(d.cell_half[a] > 0))
+      throw std::runtime_error(where + ": CELL and FD_GRID must be positive");
+  if (d.bc < 1 || d.bc > 4) throw std::runtime_error(where + ": BOUNDARY_CONDITION must be 1..4");
+  if (d.n_qp < 1 || d.n_qp > 64) throw std::runtime_error(where + ": LANCZOS_DEGREE must be 1..64");
+  if (!(d.rcut > 0)) throw std::runtime_error(where + ": RADIUS_TRUNC must be positive");
+}
+
+void check_psd(const Psd &p, const std::string &where) {
+  if (p.lmax < 0 || p.lmax > 3) throw std::runtime_error(where + ": lmax must be 0..3");
+  if (p.lloc < 0 || p.lloc > p.lmax)
+    throw std::runtime_error(where + ": PSEUDOPOTENTIAL_LOCAL out of range");
+  for (int l = 0; l <= p.lmax; l++)
+    if (l != p.lloc && !p.has_u[l]) throw std::runtime_error(where + ": missing wave function for l");
 }
 
 void parse_inpt(Deck &d, const std::string &path) {
@@ -77,12 +96,7 @@ void parse_inpt(Deck &d, const std::string &path) {
     if (it != handlers.end()) it->second();
   }
   if (ntype <= 0) throw std::runtime_error(path + ": NTYPE missing");
-  for (int a = 0; a < 3; a++)
-    if (d.grid[a] < 2 || !(d.cell_half[a] > 0))
-      throw std::runtime_error(path + ": CELL and FD_GRID must be positive");
-  if (d.bc < 1 || d.bc > 4) throw std::runtime_error(path + ": BOUNDARY_CONDITION must be 1..4");
-  if (d.n_qp < 1 || d.n_qp > 64) throw std::runtime_error(path + ": LANCZOS_DEGREE must be 1..64");
-  if (!(d.rcut > 0)) throw std::runtime_error(path + ": RADIUS_TRUNC must be positive");
+  check_deck(d, path);
 }
 
 void parse_ion(Deck &d, const std::string &path) {
@@ -177,6 +191,78 @@ Psd parse_psd(const std::string &path, const std::string &type_name, int lloc) {
 }
 
 }  // namespace
+
+Deck deck_from_system(const ::sq_system_desc &sys) {
+  const std::string where = "sq_system_desc";
+  Deck d;
+  if (sys.fd_order < 2 || sys.fd_order % 2 || sys.fd_order / 2 != kStencilHalf)
+    throw std::runtime_error(where + ": FD_ORDER must be " + std::to_string(2 * kStencilHalf));
+  d.half_order = sys.fd_order / 2;
+  d.bc = sys.bc;
+  for (int a = 0; a < 3; a++) {
+    d.cell_half[a] = sys.cell_half[a];
+    d.grid[a] = sys.grid[a];
+  }
+  d.beta = sys.beta;
+  d.rcut = sys.rcut;
+  d.n_qp = sys.n_qp;
+  if (sys.mixing_parameter > 0) d.mixing_parameter = sys.mixing_parameter;
+  if (sys.mixing_history > 0) d.mixing_history = sys.mixing_history;
+  if (sys.pulay_frequency > 0) d.pulay_frequency = sys.pulay_frequency;
+  if (sys.tol_scf > 0) d.tol_scf = sys.tol_scf;
+  if (sys.maxit_scf > 0) d.maxit_scf = sys.maxit_scf;
+  if (sys.reference_cutoff > 0) d.reference_cutoff = sys.reference_cutoff;
+  check_deck(d, where);
+  if (!(sys.beta > 0)) throw std::runtime_error(where + ": BETA must be positive");
+  if (sys.n_types <= 0 || sys.n_types > kMaxTypes || !sys.psd)
+    throw std::runtime_error(where + ": NTYPE must be 1..8 with a psd per type");
+  if (sys.n_atoms <= 0 || !sys.atom_type || !sys.atom_xyz)
+    throw std::runtime_error(where + ": atoms missing");
+  for (int t = 0; t < sys.n_types; t++) {
+    const sq_psd_desc &in = sys.psd[t];
+    const std::string w = where + " type " + std::to_string(t);
+    if (in.n_r < 3 || !in.r || in.r[0] != 0.0)
+      throw std::runtime_error(w + ": radial grid of at least 3 points starting at r = 0");
+    for (int i = 1; i < in.n_r; i++)
+      if (!(in.r[i] > in.r[i - 1])) throw std::runtime_error(w + ": radial grid must increase");
+    Psd p;
+    p.name = "type" + std::to_string(t);
+    p.lmax = in.lmax;
+    p.lloc = in.lloc;
+    p.zval = in.valence;
+    p.r.assign(in.r, in.r + in.n_r);
+    p.rho_atom.assign(in.n_r, 0.0);
+    if (in.rho_atom) p.rho_atom.assign(in.rho_atom, in.rho_atom + in.n_r);
+    for (int l = 0; l < 4; l++) {
+      p.V[l].assign(in.n_r, 0.0);
+      p.U[l].assign(in.n_r, 0.0);
+      if (l <= in.lmax) {
+        if (!in.V[l]) throw std::runtime_error(w + ": V_l missing for l <= lmax");
+        p.V[l].assign(in.V[l], in.V[l] + in.n_r);
+        if (l != in.lloc && in.U[l]) {
+          p.U[l].assign(in.U[l], in.U[l] + in.n_r);
+          p.has_u[l] = true;
+          p.rc[l] = in.rc[l];
+        }
+      }
+    }
+    check_psd(p, w);
+    p.vloc = p.V[p.lloc];
+    d.psd.push_back(p);
+    d.lloc.push_back(in.lloc);
+    d.psd_file.push_back("");
+    d.type_name.push_back(p.name);
+    d.type_valence.push_back(in.valence);
+  }
+  for (int i = 0; i < sys.n_atoms; i++) {
+    const int t = sys.atom_type[i];
+    if (t < 0 || t >= sys.n_types) throw std::runtime_error(where + ": atom type out of range");
+    d.atom_type.push_back(t);
+    for (int c = 0; c < 3; c++) d.atom_xyz.push_back(sys.atom_xyz[3 * i + c]);
+    d.n_electrons += sys.psd[t].valence;
+  }
+  return d;
+}
 
 Deck read_deck(const std::string &dir, const std::string &name) {
   Deck d;

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+struct sq_system_desc;  // sq_gb300.h
+
 namespace sq {
 
 constexpr int kMaxTypes = 8;
@@ -115,6 +117,9 @@ struct Deck {
 };
 
 Deck read_deck(const std::string &dir, const std::string &name);
+// The same Deck from values in memory (sq_system_desc of sq_gb300.h), checked as the readers
+// check the files.
+Deck deck_from_system(const ::sq_system_desc &sys);
 
 // Host setup result: everything copied to the device.
 struct Setup {

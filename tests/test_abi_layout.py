@@ -32,9 +32,11 @@ def _probe(tmp_path, structs):
 
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="needs gcc")
 def test_ctypes_mirrors_match_the_header(tmp_path):
-    from sqminiapp_gb300.capi import SqInfo, SqOptions, SqScfOptions, SqScfResult
+    from sqminiapp_gb300.capi import (SqInfo, SqOptions, SqPsdDesc, SqScfOptions, SqScfResult,
+                                      SqSystemDesc)
     mirrors = {"sq_options": SqOptions, "sq_info": SqInfo, "sq_scf_options": SqScfOptions,
-               "sq_scf_result": SqScfResult}
+               "sq_scf_result": SqScfResult, "sq_psd_desc": SqPsdDesc,
+               "sq_system_desc": SqSystemDesc}
     c = _probe(tmp_path, {n: [f for f, _ in m._fields_] for n, m in mirrors.items()})
     for n, m in mirrors.items():
         assert c[(n, "sizeof")] == ctypes.sizeof(m), n
