@@ -325,6 +325,29 @@ typedef struct sq_scf_result {
                               with FP32 Lanczos vectors (their residual noise floor is ~1e-5) */
 } sq_scf_result;
 
+/* ---- One SCF iteration with the FD nodes sharded over ranks, one GPU per rank ----
+ * The reference splits the nodes of one cell over MPI ranks (DMDACreate3d on
+ * PETSC_COMM_WORLD, src/lsdft_initObjs.cc:132-133; each rank loops over its corner block,
+ * src/lsdft_scf.cc:47-62).  Here every rank holds the whole cell (handle + sq_scf_begin with
+ * the same options and start density, so the replicated fields stay identical), runs the SQ
+ * pass on its node range only, and the caller supplies the three exchanges with its own
+ * collectives (the Python driver sqminiapp_gb300.sharding.ShardedSCF uses torch.distributed):
+ *   1. sq_scf_shard_sq: potential of rho_in (replicated), then Lanczos + quadrature of nodes
+ *      [node_begin, node_end); minmax[2] = this range's smallest and largest Ritz value;
+ *   2. the Fermi level from sq_scf_shard_counts (this range's electron counts at k trial
+ *      levels, summed over ranks by the caller), as many rounds as the search needs;
+ *   3. sq_scf_shard_density: this range's node densities (HOST rho_local[node_end-node_begin])
+ *      and sums[2] = its partial band energy 2 sum w lambda f and entropy sum
+ *      2 sum w [f ln f + (1-f) ln(1-f)] (summed over ranks; -TS is the second sum / beta);
+ *   4. sq_scf_shard_finish with the gathered full HOST rho_out[n_nodes] and the summed
+ *      scalars: residual, free energy and Periodic-Pulay mixing, replicated on every rank.
+ * No call waits on another rank. */
+sq_status sq_scf_shard_sq(sq_handle *h, long node_begin, long node_end, double *minmax);
+sq_status sq_scf_shard_counts(sq_handle *h, int k, const double *lambda_f, double *counts);
+sq_status sq_scf_shard_density(sq_handle *h, double lambda_f, double *rho_local, double *sums);
+sq_status sq_scf_shard_finish(sq_handle *h, const double *rho_out, double lambda_f, double e_band,
+                              double ts, sq_scf_result *result);
+
 /* Host-only report of a periodic deck's fixed SCF fields (no GPU touched): pseudocharges
  * b[n_nodes], atomic-superposition density rho0[n_nodes], the Poisson symbol green on the
  * R2C half grid [Nz][Ny][Nx/2+1], and scalars[4] = E_self, E_self of the reference

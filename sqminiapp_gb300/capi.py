@@ -106,6 +106,11 @@ SIGNATURES = {
     "sq_tridiag_nodes_and_weights": (ctypes.c_int, [_dp, _dp, _l, ctypes.c_int, _dp, _dp, _dp,
                                                     _dp, ctypes.c_int]),
     "sq_fermi_timeout_selftest": (ctypes.c_int, [ctypes.c_int]),
+    "sq_scf_shard_sq": (ctypes.c_int, [_vp, _l, _l, _dp]),
+    "sq_scf_shard_counts": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp]),
+    "sq_scf_shard_density": (ctypes.c_int, [_vp, ctypes.c_double, _dp, _dp]),
+    "sq_scf_shard_finish": (ctypes.c_int, [_vp, _dp, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.POINTER(SqScfResult)]),
     "sq_scf_begin": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _dp]),
     "sq_scf_begin_device": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfOptions), _vp]),
     "sq_scf_step": (ctypes.c_int, [_vp, ctypes.POINTER(SqScfResult)]),

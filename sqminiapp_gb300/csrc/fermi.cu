@@ -230,7 +230,70 @@ __global__ void sum_partials_kernel(const double *__restrict__ partial, int n,
   }
 }
 
+// Node densities, band energy and entropy term of a given Fermi level (the last phase of
+// fermi_kernel on its own): part[2 * block] = (2 sum w lambda f, 2 sum w s(f)) per CTA.
+__global__ void __launch_bounds__(kCountBlock)
+    density_energy_kernel(const double *__restrict__ lambda, const double *__restrict__ w,
+                          long long n_nodes, int nqp, double beta, double lf, double dV,
+                          double *__restrict__ rho, double *__restrict__ part) {
+  __shared__ double red[2][kCountBlock / 32];
+  double eb = 0.0, ent = 0.0;
+  for (long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x; node < n_nodes;
+       node += (long long)gridDim.x * blockDim.x) {
+    double r = 0.0;
+    for (int q = 0; q < nqp; q++) {
+      const long long e = node * nqp + q;
+      const double f = fermi_dirac(beta, lambda[e], lf);
+      r += w[e] * f;
+      eb += 2.0 * w[e] * lambda[e] * f;
+      double sv = 0.0;
+      if (f > 0.0 && f < 1.0) sv = f * log(f) + (1.0 - f) * log(1.0 - f);
+      ent += 2.0 * w[e] * sv;
+    }
+    if (rho) rho[node] = 2.0 * r / dV;
+  }
+  eb = warp_sum_d(eb);
+  ent = warp_sum_d(ent);
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = eb;
+    red[1][threadIdx.x >> 5] = ent;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < kCountBlock / 32; i++) {
+      a += red[0][i];
+      b += red[1][i];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+__global__ void sum_pairs_kernel(const double *__restrict__ part, int n, double *__restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < n; i++) {
+      a += part[2 * i];
+      b += part[2 * i + 1];
+    }
+    out[0] = a;
+    out[1] = b;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_density_energy(const double *lambda, const double *w, long long n_nodes, int nqp,
+                                  double beta, double lf, double dV, double *rho, double *partial,
+                                  int grid, double *out, cudaStream_t s) {
+  density_energy_kernel<<<grid, kCountBlock, 0, s>>>(lambda, w, n_nodes, nqp, beta, lf, dV, rho,
+                                                     partial);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  sum_pairs_kernel<<<1, 32, 0, s>>>(partial, grid, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_electron_count(const double *lambda, const double *w, long long n_nodes,
                                   int nqp, double beta, double lf, double *partial, int grid,

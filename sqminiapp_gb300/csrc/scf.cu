@@ -289,6 +289,9 @@ struct ScfState {
   bool converged = false;
   std::vector<double> hist_F, hist_err;
   sq_scf_result last{};
+  // a sharded iteration in progress (sq_scf_shard_*): this rank's node range, its start time
+  long long shard_b = 0, shard_e = 0;
+  std::chrono::steady_clock::time_point shard_t0;
   // CUDA graph of an iteration's device part (Poisson, potential, SQ pass)
   bool use_graph = false;
   cudaGraphExec_t graph_exec = nullptr;
@@ -458,6 +461,9 @@ void begin(sq_handle *h, const sq_scf_options *o, const double *rho_init, bool r
   ck(cudaStreamSynchronize(st), "sync");
 }
 
+sq_status finish(sq_handle *h, sq_scf_result *res, cudaStream_t st, double lambda_f,
+                 double e_band, double ts, std::chrono::steady_clock::time_point t0);
+
 sq_status step(sq_handle *h, sq_scf_result *res, cudaStream_t st) {
   ScfState &s = *h->scf;
   const Deck &d = h->deck;
@@ -512,13 +518,27 @@ sq_status step(sq_handle *h, sq_scf_result *res, cudaStream_t st) {
                   s.fermi_tol, h->fermi_maxit, s.d_rho_out, h->d_fermi_out, h->d_fermi_scratch,
                   h->d_bar, h->d_status, h->fermi_grid, st),
      "fermi");
-  double fo[4], es[3];
+  double fo[4];
   ck(cudaMemcpyAsync(fo, h->d_fermi_out, sizeof(fo), cudaMemcpyDeviceToHost, st), "fermi D2H");
-  ck(cudaMemcpyAsync(es, s.d_sums + kMaxSums - 3, sizeof(es), cudaMemcpyDeviceToHost, st), "sums D2H");
   rs = device_status(h, st);
   if (rs != SQ_OK) return rs;
+  return finish(h, res, st, fo[0], fo[1], fo[2], t0);
+}
+
+// Everything of an iteration after rho_out, lambda_f, e_band and -TS are known (rho_out in
+// s.d_rho_out, the exchange-correlation sums of the potential in the last three sums): the
+// residual, the free energy, the history and the Periodic-Pulay update of rho_in.
+sq_status finish(sq_handle *h, sq_scf_result *res, cudaStream_t st, double lambda_f,
+                 double e_band, double ts, std::chrono::steady_clock::time_point t0) {
+  ScfState &s = *h->scf;
+  const Deck &d = h->deck;
+  const double dV = h->setup.dV;
+  const double fo[3] = {lambda_f, e_band, ts};
+  double es[3];
+  ck(cudaMemcpyAsync(es, s.d_sums + kMaxSums - 3, sizeof(es), cudaMemcpyDeviceToHost, st), "sums D2H");
+  ck(cudaStreamSynchronize(st), "sync");
   double kt[2] = {0, 0};
-  {
+  if (h->ev_valid) {
     float a = 0, b = 0;
     ck(cudaEventElapsedTime(&a, h->ev[0], h->ev[1]), "elapsed");
     ck(cudaEventElapsedTime(&b, h->ev[1], h->ev[2]), "elapsed");
@@ -645,6 +665,101 @@ sq_status sq_scf_step(sq_handle *h, sq_scf_result *result) {
   return guarded([&] {
     ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
     return step(h, result, h->own_stream);
+  });
+}
+
+// ---- one SCF iteration with the nodes sharded over ranks (see sq_gb300.h) ----
+sq_status sq_scf_shard_sq(sq_handle *h, long node_begin, long node_end, double *minmax) {
+  if (!h || !minmax) return fail(SQ_BAD_INPUT, "null argument");
+  if (!h->scf) return fail(SQ_BAD_INPUT, "sq_scf_begin has not been called");
+  return guarded([&] {
+    ScfState &s = *h->scf;
+    if (node_begin < 0 || node_end > s.ng || node_end <= node_begin)
+      return fail(SQ_BAD_INPUT, "node range outside the grid");
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t st = h->own_stream;
+    s.shard_t0 = std::chrono::steady_clock::now();
+    const long long n = node_end - node_begin;
+    ensure_quadrature_buffers(h, n);
+    poisson(s, s.d_rho_in, s.d_phi, st);
+    potential_kernel<<<kRedBlocks, kBlock, 0, st>>>(s.d_rho_in, s.d_phi, s.d_b, s.d_vxc, s.d_veff,
+                                                    s.ng, s.d_part);
+    ck(cudaGetLastError(), "potential");
+    finish_sums<<<1, 256, 0, st>>>(s.d_part, kRedBlocks, 3, s.d_sums + kMaxSums - 3);
+    ck(cudaGetLastError(), "finish sums");
+    sq_status rs = run_device(h, s.d_veff, 0.0, node_begin, node_end, h->d_lambda, h->d_w,
+                              h->d_lmin, h->d_lmax, st);
+    if (rs != SQ_OK) return rs;
+    rs = device_status(h, st);
+    if (rs != SQ_OK) return rs;
+    std::vector<double> lo(n), hi(n);
+    ck(cudaMemcpy(lo.data(), h->d_lmin, sizeof(double) * n, cudaMemcpyDeviceToHost), "D2H");
+    ck(cudaMemcpy(hi.data(), h->d_lmax, sizeof(double) * n, cudaMemcpyDeviceToHost), "D2H");
+    minmax[0] = *std::min_element(lo.begin(), lo.end());
+    minmax[1] = *std::max_element(hi.begin(), hi.end());
+    s.shard_b = node_begin;
+    s.shard_e = node_end;
+    return SQ_OK;
+  });
+}
+
+sq_status sq_scf_shard_counts(sq_handle *h, int k, const double *lambda_f, double *counts) {
+  if (!h || !lambda_f || !counts || k <= 0) return fail(SQ_BAD_INPUT, "null argument or k <= 0");
+  if (!h->scf || h->scf->shard_e <= h->scf->shard_b)
+    return fail(SQ_BAD_INPUT, "sq_scf_shard_sq has not been called");
+  return guarded([&] {
+    ScfState &s = *h->scf;
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t st = h->own_stream;
+    const int grid = 4 * h->num_sms;
+    for (int i = 0; i < k; i++) {
+      ck(launch_electron_count(h->d_lambda, h->d_w, s.shard_e - s.shard_b, h->lp.nqp,
+                               h->info.beta, lambda_f[i], h->d_fermi_scratch, grid,
+                               h->d_fermi_out, st),
+         "electron count");
+      ck(cudaMemcpyAsync(counts + i, h->d_fermi_out, sizeof(double), cudaMemcpyDeviceToHost, st),
+         "D2H");
+    }
+    ck(cudaStreamSynchronize(st), "sync");
+    return SQ_OK;
+  });
+}
+
+sq_status sq_scf_shard_density(sq_handle *h, double lambda_f, double *rho_local, double *sums) {
+  if (!h || !rho_local || !sums) return fail(SQ_BAD_INPUT, "null argument");
+  if (!h->scf || h->scf->shard_e <= h->scf->shard_b)
+    return fail(SQ_BAD_INPUT, "sq_scf_shard_sq has not been called");
+  return guarded([&] {
+    ScfState &s = *h->scf;
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t st = h->own_stream;
+    const long long n = s.shard_e - s.shard_b;
+    const int grid = 2 * h->num_sms;
+    ck(launch_density_energy(h->d_lambda, h->d_w, n, h->lp.nqp, h->info.beta, lambda_f,
+                             h->setup.dV, s.d_rho_out + s.shard_b, h->d_fermi_scratch, grid,
+                             h->d_fermi_out, st),
+       "density");
+    ck(cudaMemcpyAsync(rho_local, s.d_rho_out + s.shard_b, sizeof(double) * n,
+                       cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaMemcpyAsync(sums, h->d_fermi_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaStreamSynchronize(st), "sync");
+    return SQ_OK;
+  });
+}
+
+sq_status sq_scf_shard_finish(sq_handle *h, const double *rho_out, double lambda_f, double e_band,
+                              double ts, sq_scf_result *result) {
+  if (!h || !rho_out) return fail(SQ_BAD_INPUT, "null argument");
+  if (!h->scf || h->scf->shard_e <= h->scf->shard_b)
+    return fail(SQ_BAD_INPUT, "sq_scf_shard_sq has not been called");
+  return guarded([&] {
+    ScfState &s = *h->scf;
+    ck(cudaSetDevice(h->opt.device), "cudaSetDevice");
+    cudaStream_t st = h->own_stream;
+    ck(cudaMemcpyAsync(s.d_rho_out, rho_out, sizeof(double) * s.ng, cudaMemcpyHostToDevice, st),
+       "rho_out H2D");
+    s.shard_b = s.shard_e = 0;
+    return finish(h, result, st, lambda_f, e_band, ts, s.shard_t0);
   });
 }
 

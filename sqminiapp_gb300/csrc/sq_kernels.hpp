@@ -77,6 +77,13 @@ cudaError_t launch_fermi_timeout_selftest(const double *lambda, const double *w,
                                           unsigned *barrier, int *status, int grid,
                                           cudaStream_t s);
 
+// Node densities rho = (2/dV) sum_q w f (rho may be NULL) and out[0..1] = band energy
+// 2 sum w lambda f and 2 sum w [f ln f + (1-f) ln(1-f)] at a given Fermi level;
+// `partial` holds 2 * grid doubles.
+cudaError_t launch_density_energy(const double *lambda, const double *w, long long n_nodes, int nqp,
+                                  double beta, double lf, double dV, double *rho, double *partial,
+                                  int grid, double *out, cudaStream_t s);
+
 // N_e(lf) = 2 sum w f(lambda - lf) over n_nodes*nqp entries; `partial` holds `grid` doubles.
 cudaError_t launch_electron_count(const double *lambda, const double *w, long long n_nodes,
                                   int nqp, double beta, double lf, double *partial, int grid,
