@@ -133,6 +133,10 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
   if (precision == 32) {
     if (p.layout & kLayoutQuad) {  // corrected operator, full records, P and U on chip
       if (faithful || !u_smem || (p.layout & ~kLayoutQuad)) return cudaErrorInvalidValue;
+      // status[1]: the kernel's node queue (nodes past the first round go to whichever CTA
+      // finishes first)
+      const cudaError_t e = cudaMemsetAsync(status + 1, 0, sizeof(int), s);
+      if (e != cudaSuccess) return e;
       return launch_lanczos_f32_quad(mask, p, grid, block, smem, s, veff_ext, images, tables,
                                      proj_scratch, ab, status);
     }

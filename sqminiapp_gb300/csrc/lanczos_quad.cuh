@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(MAXT, 1)
   int *kept = pref + maxi + 1;
   int *koff = kept + maxi;      // maxi + 1
   int *slot_first = koff + maxi + 1;  // first image of every slot (images sorted by atom)
-  int *cnt = slot_first + maxi;  // [0] images, [1] slots, [2] overflow
+  int *cnt = slot_first + maxi;  // [0] images, [1] slots, [2] overflow, [3] next node
 
   typename Rec::vec_t *rec = reinterpret_cast<typename Rec::vec_t *>(
       proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
@@ -205,7 +205,10 @@ __global__ void __launch_bounds__(MAXT, 1)
   const int x0 = 4 * ql;
   const bool in1 = x0 + 1 < nx, in2 = x0 + 2 < nx, in3 = x0 + 3 < nx;  // x0 < nx always
 
-  for (long long node = p.node_begin + blockIdx.x; node < p.node_end; node += gridDim.x) {
+  // nodes: the first round one per CTA, then a queue (status[1], zeroed before the launch):
+  // per-node cost varies with the atoms near the node, so CTAs take nodes as they finish
+  for (long long node = p.node_begin + blockIdx.x; node < p.node_end;
+       node = p.node_begin + gridDim.x + cnt[3]) {
     const int I = (int)(node % p.Nx);
     const int J = (int)((node / p.Nx) % p.Ny);
     const int K = (int)(node / ((long long)p.Nx * p.Ny));
@@ -283,6 +286,9 @@ __global__ void __launch_bounds__(MAXT, 1)
       }
     }
     __syncthreads();
+    // the next node, read by every thread after this node's last barrier (the previous value
+    // was read before the barrier above)
+    if (threadIdx.x == 0) cnt[3] = atomicAdd(status + 1, 1);
     const int n_img = cnt[0], n_slot = cnt[1];
     if (cnt[2] || pref[n_img] > p.proj_cap) {  // capacity exceeded: report, NaN coefficients
       if (threadIdx.x == 0) atomicOr(status, kStatusCapacity);
