@@ -54,12 +54,14 @@ typedef struct sq_options {
    * FP64 and the faithful operator always use the full format. */
   int list_format;
   /* FP32 Lanczos kernel: 0 automatic (the split-pass kernel where it applies: corrected
-   * operator, cubes at most 32 points wide, both vectors and the full lists fit), 1 the
-   * single-pass kernel, 2 the split-pass kernel (SQ_BAD_INPUT where it does not apply). */
+   * operator, the full lists in L2, both vectors on one CTA -- or, for larger cubes such as
+   * 31^3 and 33^3, on a cluster of two CTAs per node), 1 the single-pass kernel, 2 the
+   * split-pass kernel (SQ_BAD_INPUT where it does not apply). */
   int kernel;
   /* Split-pass kernel tile: z-ranges per cube row in the z pass and y-ranges per plane in the
    * y pass (threads = ceil(nx/4) * max(ny,nz) * tile); 0 automatic (the engine's autotuner
-   * times the candidates on the first call and keeps the fastest). */
+   * times the candidates on the first call and keeps the fastest).  The two-CTA form runs
+   * one tile and needs 0. */
   int tile;
 } sq_options;
 
@@ -89,8 +91,8 @@ typedef struct sq_info {
   /* Lanczos kernel configuration (0 from sq_describe_deck): vector layout flags (1 = zero rows
    * between z-planes, FP32; 2 = cubes wider than 32 points, FP32; 4 = rows without zero
    * columns, FP64; 8 = compact projector list; 16 = split-pass kernel over 16-byte quads,
-   * FP32), U on chip (1) or in global scratch (0), threads per CTA, shared memory bytes per
-   * CTA. */
+   * FP32; 32 = with 16, a cluster of two CTAs per node, the cube split in z), U on chip (1) or
+   * in global scratch (0), threads per CTA, shared memory bytes per CTA. */
   int kernel_layout;
   int kernel_u_on_chip;
   int kernel_threads;

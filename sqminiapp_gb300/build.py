@@ -25,6 +25,7 @@ SOURCES = {
     "lanczos_f32n.cu": ["-Xptxas", "-v"],
     "lanczos_f32c.cu": ["-Xptxas", "-v"],
     "lanczos_f32q.cu": ["-Xptxas", "-v"],
+    "lanczos_f32p.cu": ["-Xptxas", "-v"],
     "lanczos_f64.cu": ["-Xptxas", "-v"],
     "lanczos_f64x.cu": ["-Xptxas", "-v"],
     "quadrature.cu": ["-fmad=false"],

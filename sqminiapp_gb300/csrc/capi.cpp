@@ -308,13 +308,14 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
   h->u_smem = false;
   p.layout = 0;
   p.zchunks = 1;
+  p.ychunks = 1;
+  p.zsplit = 0;
   p.vq_row = 4 * ((p.EX + 6 + 3) / 4);  // the row of a quad-aligned Veff copy (see below)
   p.vq_copy_stride = (long long)p.vq_row * p.EY * p.EZ;
   h->quad = false;
   if (h->opt.kernel < 0 || h->opt.kernel > 2 || h->opt.tile < 0)
     throw std::invalid_argument("sq_options.kernel must be 0, 1 or 2 and tile >= 0");
-  if (h->opt.precision == 32 && !faithful && !wide && h->opt.kernel != 1 &&
-      h->opt.list_format != 2) {
+  if (h->opt.precision == 32 && !faithful && h->opt.kernel != 1 && h->opt.list_format != 2) {
     // split-pass kernel over 16-byte quads: P and U on chip as [nz][ny][4 ceil(nx/4)], full
     // projector records, which must stay in L2 together (152 CTAs' lists)
     sq::LanczosParams q = p;
@@ -325,17 +326,38 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
     const double list_bytes = (double)h->num_sms * projector_points_per_node(s, d) *
                               kept_fraction(s) *
                               (double)sq::proj_record_bytes(4, false, p.union_mask, false);
-    if (threads <= sq::kQuadMaxThreads && sq::lanczos_quad_smem_bytes(q) <= (size_t)smem_optin &&
+    if (!wide && threads <= sq::kQuadMaxThreads &&
+        sq::lanczos_quad_smem_bytes(q) <= (size_t)smem_optin &&
         (h->opt.list_format == 1 || list_bytes <= 0.75 * (double)l2_bytes)) {
       p = q;
       h->quad = true;
       h->u_smem = true;
       h->block = threads;
+    } else if (h->opt.tile == 0 && p.nz >= 2 * sq::kStencilHalf + 2) {
+      // the same kernel on a pair of CTAs per node, the cube split in z: each holds its half
+      // of U and its half of P plus 6 halo planes; each streams its half of the list
+      q.layout = sq::kLayoutQuad | sq::kLayoutPair;
+      q.zsplit = (p.nz + 1) / 2;
+      q.zchunks = 1;
+      q.ychunks = 2;
+      int pt = sq::lanczos_quad_threads(q);
+      if (pt > sq::kPairThreads) {
+        q.ychunks = 1;
+        pt = sq::lanczos_quad_threads(q);
+      }
+      if (pt <= sq::kPairThreads && sq::lanczos_quad_smem_bytes(q) <= (size_t)smem_optin &&
+          (h->opt.list_format == 1 || 0.5 * list_bytes <= 0.75 * (double)l2_bytes)) {
+        p = q;
+        h->quad = true;
+        h->u_smem = true;
+        h->block = pt;
+        h->tuned = true;  // one tile
+      }
     }
   }
   if (h->opt.kernel == 2 && !h->quad)
     throw std::invalid_argument("the split-pass FP32 kernel does not apply to this cell and options "
-                                "(FP32, corrected operator, cubes at most 32 wide, lists in L2)");
+                                "(FP32, corrected operator, P and U on one or two CTAs, lists in L2)");
   if (h->quad) {
     // nothing else to choose: layout, threads and lists are fixed above
   } else if (h->opt.precision == 32) {
@@ -410,6 +432,11 @@ void build_engine(sq_handle *h) {
      "smem optin");
   ck(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, h->opt.device), "L2 size");
   plan_engine(h, smem_optin, l2);
+  if (h->lp.layout & sq::kLayoutPair) {  // no more pairs than fit on the device at once
+    const int pairs = sq::lanczos_quad_pair_clusters(h->lp, h->block, h->smem);
+    if (pairs < 1) throw std::runtime_error("no cluster of two CTAs fits this kernel on the device");
+    h->grid = std::min(h->grid / 2, pairs) * 2;
+  }
   ck(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking), "stream");
   for (auto &e : h->ev) ck(cudaEventCreate(&e), "event");
   const sq::Setup &s = h->setup;
@@ -502,7 +529,10 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
   p.node_end = ne;
   ck(cudaMemsetAsync(h->d_status, 0, sizeof(int), s), "status reset");
   ck(sq::launch_veff_extend(d_veff, veff_const, h->d_veff_ext, h->opt.precision, p, s), "veff");
-  const int grid = (int)std::min<long long>(grid_limit > 0 ? std::min(grid_limit, h->grid) : h->grid, n);
+  int grid = (int)std::min<long long>(grid_limit > 0 ? std::min(grid_limit, h->grid) : h->grid, n);
+  if (p.layout & sq::kLayoutPair)  // two CTAs per node: an even grid, one pair per node at most
+    grid = 2 * (int)std::max<long long>(
+                   1, std::min<long long>((grid_limit > 0 ? std::min(grid_limit, h->grid) : h->grid) / 2, n));
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   ck(cudaStreamIsCapturing(s, &cap), "capture status");
   const bool timed = cap == cudaStreamCaptureStatusNone;  // no timing events inside a graph

@@ -123,6 +123,10 @@ cudaError_t launch_lanczos_f32_quad(int mask, const LanczosParams &p, int grid, 
                                     size_t smem, cudaStream_t s, const void *veffq,
                                     const ImageMeta *images, const void *tables,
                                     void *proj_scratch, double *ab, int *status);
+cudaError_t launch_lanczos_f32_pair(int mask, const LanczosParams &p, int grid, int block,
+                                    size_t smem, cudaStream_t s, const void *veffq,
+                                    const ImageMeta *images, const void *tables,
+                                    void *proj_scratch, double *ab, int *status);
 
 cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful, bool u_smem,
                            int grid, int block, size_t smem, cudaStream_t s, const void *veff_ext,
@@ -132,7 +136,11 @@ cudaError_t launch_lanczos(const LanczosParams &p, int precision, bool faithful,
   const bool gap = (p.layout & kLayoutYGap) != 0;
   if (precision == 32) {
     if (p.layout & kLayoutQuad) {  // corrected operator, full records, P and U on chip
-      if (faithful || !u_smem || (p.layout & ~kLayoutQuad)) return cudaErrorInvalidValue;
+      if (faithful || !u_smem || (p.layout & ~(kLayoutQuad | kLayoutPair)))
+        return cudaErrorInvalidValue;
+      if (p.layout & kLayoutPair)
+        return launch_lanczos_f32_pair(mask, p, grid, block, smem, s, veff_ext, images, tables,
+                                       proj_scratch, ab, status);
       // status[1]: the kernel's node queue (nodes past the first round go to whichever CTA
       // finishes first)
       const cudaError_t e = cudaMemsetAsync(status + 1, 0, sizeof(int), s);

@@ -5,18 +5,27 @@
 namespace sq {
 
 int lanczos_quad_threads(const LanczosParams &p) {
-  // pitch/4 threads per row (pass A) or plane (pass B), zchunks ranges each
+  // pitch/4 threads per row (pass A) or plane (pass B), zchunks ranges each (a pair: rows
+  // over the owned planes, zchunks z-ranges; owned planes, ychunks y-ranges)
   // at least two warps: warp 0 builds the per-node image list while the others clear P and U
-  const int groups = std::max(p.ny, p.nz) * p.zchunks;
+  const int groups = (p.layout & kLayoutPair)
+                         ? std::max(p.ny * p.zchunks, lq::pair_u_planes(p.nz, p.zsplit) * p.ychunks)
+                         : std::max(p.ny, p.nz) * p.zchunks;
   return std::max(64, 32 * (((p.pitch / 4) * groups + 31) / 32));
 }
 
 size_t lanczos_quad_smem_bytes(const LanczosParams &p) {
-  const size_t nc = (size_t)p.nz * lq::quad_plane_floats(p.ny, p.pitch);
+  const bool pair = (p.layout & kLayoutPair) != 0;
+  const size_t ps = lq::quad_plane_floats(p.ny, p.pitch);
   const int nlm = mask_nlm(kernel_mask(p.union_mask));
-  size_t b = sizeof(float) * 2 * nc;                          // P, U
+  size_t b = pair ? sizeof(float) * ps * (lq::pair_p_planes(p.nz, p.zsplit) +
+                                          lq::pair_u_planes(p.nz, p.zsplit))
+                  : sizeof(float) * 2 * ps * p.nz;           // P, U
   b += sizeof(double) * (2 * lk::kMaxWarps + 128);           // a_k / b_k partials, a[], b[]
   b += sizeof(float) * (2 * (size_t)p.max_img + lk::kMaxWarps) * nlm;  // c partials, alpha
+  if (pair)  // both CTAs' c, an 8-byte alignment, projector a_k partials, capacity flags
+    b += sizeof(float) * 2 * (size_t)p.max_img * nlm + 8 + sizeof(float) * 2 * lk::kMaxWarps +
+         sizeof(int) * 4;
   b += sizeof(int) * (9 * (size_t)p.max_img + 2) + sizeof(int) * 4;    // per-node image lists
   return b;
 }

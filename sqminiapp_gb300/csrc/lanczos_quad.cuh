@@ -42,6 +42,8 @@
 // critical path and converts to double only to store a_k and b_k.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "lanczos_kernel.cuh"
 
 namespace sq {
@@ -132,28 +134,63 @@ __host__ __device__ constexpr int quad_plane_floats(int ny, int pitch) {
   return ny * pitch + ((pitch - ny * pitch) % 32 + 32) % 32;
 }
 
-template <int MASK, int MAXT, bool ISO>
-__global__ void __launch_bounds__(MAXT, 1)
-    lanczos_quad_kernel(const __grid_constant__ LanczosParams p, const float *__restrict__ veffq,
-                        const ImageMeta *__restrict__ images, const float *__restrict__ tables,
-                        unsigned char *proj_scratch, double *__restrict__ ab_out,
-                        int *__restrict__ status) {
+// CTA pair (cube split in z at zsplit): CTA r owns planes [zo0, zo1) of P and U and keeps
+// P's planes [pz0, pz1) = its own plus O halo planes on the peer's side, which the peer writes.
+struct PairPlanes {
+  int zo0, zo1, pz0, pz1;
+};
+__host__ __device__ constexpr PairPlanes pair_planes(int nz, int zsplit, int rank) {
+  return rank == 0 ? PairPlanes{0, zsplit, 0, zsplit + O < nz ? zsplit + O : nz}
+                   : PairPlanes{zsplit, nz, zsplit - O > 0 ? zsplit - O : 0, nz};
+}
+// planes of P and of U to allocate: the larger of the two CTAs'
+__host__ __device__ constexpr int pair_p_planes(int nz, int zsplit) {
+  return (pair_planes(nz, zsplit, 0).pz1 - pair_planes(nz, zsplit, 0).pz0) >
+                 (pair_planes(nz, zsplit, 1).pz1 - pair_planes(nz, zsplit, 1).pz0)
+             ? pair_planes(nz, zsplit, 0).pz1 - pair_planes(nz, zsplit, 0).pz0
+             : pair_planes(nz, zsplit, 1).pz1 - pair_planes(nz, zsplit, 1).pz0;
+}
+__host__ __device__ constexpr int pair_u_planes(int nz, int zsplit) {
+  return zsplit > nz - zsplit ? zsplit : nz - zsplit;
+}
+
+// PAIR: one node per cluster of two CTAs (the cube split in z, see PairPlanes); else one node
+// per CTA.
+template <int MASK, int MAXT, bool ISO, bool PAIR>
+__device__ __forceinline__ void quad_body(const LanczosParams &p, const float *__restrict__ veffq,
+                                          const ImageMeta *__restrict__ images,
+                                          const float *__restrict__ tables,
+                                          unsigned char *proj_scratch, double *__restrict__ ab_out,
+                                          int *__restrict__ status) {
   constexpr int NLM = lk::Lm<MASK>::nlm;
   using Rec = lk::ProjRec<float, NLM>;
-  constexpr int kStream = lk::stream_batch<Rec::nvec * (int)sizeof(typename Rec::vec_t)>();
+  // points per lane per batch of the gather and of the scatter (all loads of a batch are in
+  // flight together; larger batches waste more lanes at the end of each image's range)
+  constexpr int kRecBytes = Rec::nvec * (int)sizeof(typename Rec::vec_t);
+  constexpr int kStreamG = kRecBytes <= 16 ? 6 : lk::stream_batch<kRecBytes>();
+  constexpr int kStreamS = kRecBytes <= 16 ? 8 : lk::stream_batch<kRecBytes>();
   const int nw = blockDim.x >> 5;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nx = p.nx, ny = p.ny, nz = p.nz, pitch = p.pitch;
   const int nq = pitch >> 2;        // quads per row
   const int PS = quad_plane_floats(ny, pitch);  // plane stride (floats)
   const int PS4 = PS >> 2;                       // plane stride (quads)
-  const int nc = nz * PS;           // floats of P (and of U)
   const int maxi = p.max_img;
+  // planes owned ([zo0, zo1): U and the list) and held of P ([pz0, pz1)); P plane z sits at
+  // local plane z - pz0, U plane z at z - zo0
+  int cr = 0;  // rank in the CTA pair
+  if constexpr (PAIR) cr = (int)cooperative_groups::this_cluster().block_rank();
+  const PairPlanes pp = PAIR ? pair_planes(nz, p.zsplit, cr) : PairPlanes{0, nz, 0, nz};
+  const int zo0 = pp.zo0, zo1 = pp.zo1, pz0 = pp.pz0, pz1 = pp.pz1, nzo = zo1 - zo0;
+  const int ncp = (PAIR ? pair_p_planes(nz, p.zsplit) : nz) * PS;  // floats of P
+  const int ncu = (PAIR ? pair_u_planes(nz, p.zsplit) : nz) * PS;  // floats of U
+  const int pofs4 = -pz0 * PS4, uofs4 = -zo0 * PS4;  // quad index shifts of planes
+  const int udelta = (zo0 - pz0) * PS;  // U index of a list point = its P index - udelta
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *P = reinterpret_cast<float *>(smem_raw);
-  float *U = P + nc;
-  unsigned char *cur = reinterpret_cast<unsigned char *>(U + nc);
+  float *U = P + ncp;
+  unsigned char *cur = reinterpret_cast<unsigned char *>(U + ncu);
   double *sab = reinterpret_cast<double *>(cur);  // a[64], b[64]
   float2 *red_a = reinterpret_cast<float2 *>(sab + 128);  // per-warp double-float partials
   float2 *red_b = red_a + kMaxWarps;
@@ -164,6 +201,20 @@ __global__ void __launch_bounds__(MAXT, 1)
   cur += sizeof(float) * (maxi + kMaxWarps) * NLM;
   float *alpha = reinterpret_cast<float *>(cur);
   cur += sizeof(float) * maxi * NLM;
+  // PAIR: the two CTAs' gathered c per (slot, lm), [rank][slot * NLM + lm] (each CTA writes
+  // its row into both), the per-warp partials of the projector part of a_k and the two
+  // CTAs' capacity flags
+  float *cx = reinterpret_cast<float *>(cur);
+  float2 *red_n = reinterpret_cast<float2 *>(cur);
+  int *xflag = reinterpret_cast<int *>(cur);
+  if constexpr (PAIR) {
+    cur += sizeof(float) * 2 * maxi * NLM;
+    cur += (8 - (reinterpret_cast<uintptr_t>(cur) & 7)) & 7;
+    red_n = reinterpret_cast<float2 *>(cur);
+    cur += sizeof(float2) * kMaxWarps;
+    xflag = reinterpret_cast<int *>(cur);
+    cur += sizeof(int) * 4;
+  }
   int *img = reinterpret_cast<int *>(cur);
   int *slot = img + maxi;
   int *slot_type = slot + maxi;
@@ -188,27 +239,29 @@ __global__ void __launch_bounds__(MAXT, 1)
   // thread -> quad of a row (pass A) / of a plane (pass B): nq consecutive threads own the
   // quads of one row or plane, so consecutive threads touch consecutive 16-byte quads
   const int grp = threadIdx.x / nq, ql = threadIdx.x - grp * nq;
-  const int nch = p.zchunks;
-  const bool qin = true;
-  // pass A: row yA, z-range [zbA, zeA)
+  const int nch = p.zchunks, nchB = PAIR ? p.ychunks : p.zchunks;
+  // pass A: row yA, z-range [zbA, zeA) of the owned planes
   const int yA = grp % ny, zcA = grp / ny;
-  const int zlen = (nz + nch - 1) / nch;
-  const int zbA = min(nz, zcA * zlen), zeA = min(nz, zbA + zlen);
-  const bool actA = qin && zcA < nch && zbA < zeA;
-  // pass B: plane zB, y-range [ybB, yeB)
-  const int zB = grp % nz, ycB = grp / nz;
-  const int ylen = (ny + nch - 1) / nch;
+  const int zlen = (nzo + nch - 1) / nch;
+  const int zbA = zo0 + min(nzo, zcA * zlen), zeA = min(zo1, zbA + zlen);
+  const bool actA = zcA < nch && zbA < zeA;
+  // pass B: owned plane zB, y-range [ybB, yeB)
+  const int zB = zo0 + grp % nzo, ycB = grp / nzo;
+  const int ylen = (ny + nchB - 1) / nchB;
   const int ybB = min(ny, ycB * ylen), yeB = min(ny, ybB + ylen);
-  const bool actB = qin && ycB < nch && ybB < yeB;
+  const bool actB = ycB < nchB && ybB < yeB;
   // x neighbours of the quad inside the row; lanes of the last quad zero its pad points
   const bool hm1 = ql >= 1, hm2 = ql >= 2, hp1 = ql + 1 < nq, hp2 = ql + 2 < nq;
   const int x0 = 4 * ql;
   const bool in1 = x0 + 1 < nx, in2 = x0 + 2 < nx, in3 = x0 + 3 < nx;  // x0 < nx always
 
   // nodes: the first round one per CTA, then a queue (status[1], zeroed before the launch):
-  // per-node cost varies with the atoms near the node, so CTAs take nodes as they finish
-  for (long long node = p.node_begin + blockIdx.x; node < p.node_end;
-       node = p.node_begin + gridDim.x + cnt[3]) {
+  // per-node cost varies with the atoms near the node, so CTAs take nodes as they finish.
+  // PAIR: node i of the cluster sequence, both CTAs alike (no queue).
+  const long long n_units = PAIR ? gridDim.x / 2 : gridDim.x;
+  const long long unit = PAIR ? blockIdx.x / 2 : blockIdx.x;
+  for (long long node = p.node_begin + unit; node < p.node_end;
+       node = PAIR ? node + n_units : p.node_begin + n_units + cnt[3]) {
     const int I = (int)(node % p.Nx);
     const int J = (int)((node / p.Nx) % p.Ny);
     const int K = (int)(node / ((long long)p.Nx * p.Ny));
@@ -244,10 +297,10 @@ __global__ void __launch_bounds__(MAXT, 1)
           type = m.type;
           start = (k == 0) || images[img[k - 1]].atom != atom;
           const TypeDesc &td = p.types[m.type];
-          const int xa = max(m.bx, Xs), ya = max(m.by, Ys), za = max(m.bz, Zs);
+          const int xa = max(m.bx, Xs), ya = max(m.by, Ys), za = max(m.bz, Zs + zo0);
           const int ex = min(m.bx + td.fx, Xs + nx) - xa;
           const int ey = min(m.by + td.fy, Ys + ny) - ya;
-          const int ez = min(m.bz + td.fz, Zs + nz) - za;
+          const int ez = max(0, min(m.bz + td.fz, Zs + zo1) - za);  // owned planes only
           npts = ex * ey * ez;
           lo = (xa - Xs) | ((ya - Ys) << 10) | ((za - Zs) << 20);
           ext = ex | (ey << 10) | (ez << 20);
@@ -280,29 +333,43 @@ __global__ void __launch_bounds__(MAXT, 1)
         cnt[2] = count > maxi;
       }
     } else {
-      for (int e = threadIdx.x - 32; e < (nc >> 2); e += blockDim.x - 32) {
-        P4[e] = zero4;
-        U4[e] = zero4;
-      }
+      for (int e = threadIdx.x - 32; e < (ncp >> 2); e += blockDim.x - 32) P4[e] = zero4;
+      for (int e = threadIdx.x - 32; e < (ncu >> 2); e += blockDim.x - 32) U4[e] = zero4;
     }
     __syncthreads();
-    // the next node, read by every thread after this node's last barrier (the previous value
-    // was read before the barrier above)
-    if (threadIdx.x == 0) cnt[3] = atomicAdd(status + 1, 1);
     const int n_img = cnt[0], n_slot = cnt[1];
-    if (cnt[2] || pref[n_img] > p.proj_cap) {  // capacity exceeded: report, NaN coefficients
+    bool overflow = cnt[2] || pref[n_img] > p.proj_cap;
+    if constexpr (PAIR) {  // both CTAs take the capacity branch together
+      if (threadIdx.x == 0) {
+        xflag[cr] = overflow;
+        *cooperative_groups::this_cluster().map_shared_rank(xflag + cr, cr ^ 1) = overflow;
+      }
+      cooperative_groups::this_cluster().sync();
+      overflow = xflag[0] || xflag[1];
+    } else {
+      // the next node, read by every thread after this node's last barrier (the previous
+      // value was read before the barrier above)
+      if (threadIdx.x == 0) cnt[3] = atomicAdd(status + 1, 1);
+    }
+    if (overflow) {  // capacity exceeded: report, NaN coefficients
       if (threadIdx.x == 0) atomicOr(status, kStatusCapacity);
-      for (int j = threadIdx.x; j < 2 * p.nqp; j += blockDim.x)
-        ab_out[(node - p.node_begin) * 2 * p.nqp + j] = __longlong_as_double(0x7ff8000000000000ll);
-      __syncthreads();
+      if (cr == 0)
+        for (int j = threadIdx.x; j < 2 * p.nqp; j += blockDim.x)
+          ab_out[(node - p.node_begin) * 2 * p.nqp + j] = __longlong_as_double(0x7ff8000000000000ll);
+      if constexpr (PAIR) cooperative_groups::this_cluster().sync();  // flags read by both
+      else __syncthreads();
       continue;
     }
-    if (threadIdx.x == 0) P[(nz - 1) / 2 * PS + (ny - 1) / 2 * pitch + (nx - 1) / 2] = 1.f;
+    {  // v_0: the unit vector at the cube centre, in every CTA that holds that plane of P
+      const int zc = (nz - 1) / 2;
+      if (threadIdx.x == 0 && zc >= pz0 && zc < pz1)
+        P[(zc - pz0) * PS + (ny - 1) / 2 * pitch + (nx - 1) / 2] = 1.f;
+    }
 
     // ---- this node's projector list: one warp per image, support points only ----
     for (int kk = warp; kk < n_img; kk += nw) {
       const lk::ImgView<float> v =
-          lk::load_view<float>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, 0, PS);
+          lk::load_view<float>(p, images, tables, img[kk], blo[kk], bext[kk], Xs, Ys, Zs, pofs4 * 4, PS);
       const int npts = pref[kk + 1] - pref[kk];
       int kept_n = 0;
       for (int q0 = 0; q0 < npts; q0 += 32) {
@@ -395,17 +462,17 @@ __global__ void __launch_bounds__(MAXT, 1)
           float acc[NLM];
 #pragma unroll
           for (int s = 0; s < NLM; s++) acc[s] = 0.f;
-          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
-            float c[kStream][NLM];
-            unsigned ix[kStream];
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStreamG) {
+            float c[kStreamG][NLM];
+            unsigned ix[kStreamG];
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
+            for (int u = 0; u < kStreamG; u++) {
               const int e = min(i0 + 32 * u, kend - 1) + shift;
               ix[u] = ridx[e];
               Rec::load(rec, e, c[u]);
             }
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
+            for (int u = 0; u < kStreamG; u++) {
               const float val = (i0 + 32 * u < kend) ? P[ix[u]] : 0.f;
 #pragma unroll
               for (int s = 0; s < NLM; s++) acc[s] = fmaf(c[u][s], val, acc[s]);
@@ -435,7 +502,7 @@ __global__ void __launch_bounds__(MAXT, 1)
 #pragma unroll
         for (int q = -O; q < O; q++) {
           const int zq = zbA + q;
-          ring[q + O + 1] = (zq >= 0 && zq < nz) ? P4c[row4 + zq * PS4] : zero4;
+          ring[q + O + 1] = (zq >= 0 && zq < nz) ? P4c[row4 + zq * PS4 + pofs4] : zero4;
         }
         // x neighbours: the upper half of quad q-2, quads q-1 and q+1, the lower half of q+2
         float2 xm2 = make_float2(0.f, 0.f), xp2 = make_float2(0.f, 0.f);
@@ -446,7 +513,7 @@ __global__ void __launch_bounds__(MAXT, 1)
         constexpr bool kPrefetch = MAXT <= 384;
         float4 nuo = zero4, ndv = zero4;
         if constexpr (kPrefetch) {
-          nuo = U4[row4 + zbA * PS4];
+          nuo = U4[row4 + zbA * PS4 + uofs4];
           ndv = __ldg(vrow + (size_t)zbA * VPS4);
         }
         for (int z0 = zbA; z0 < zeA; z0 += W) {
@@ -455,9 +522,9 @@ __global__ void __launch_bounds__(MAXT, 1)
             const int z = z0 + s;
             if (z >= zeA) break;
             const int qn = z + O;
-            ring[s] = qn < nz ? P4c[row4 + qn * PS4] : zero4;
+            ring[s] = qn < nz ? P4c[row4 + qn * PS4 + pofs4] : zero4;
 #define RING(dd) ring[(s + (dd) + O + 1) % W]
-            const int i4 = row4 + z * PS4;
+            const int i4 = row4 + z * PS4 + pofs4, iu4 = row4 + z * PS4 + uofs4;
             if (hm2) xm2 = P2c[2 * i4 - 3];
             if (hm1) xm1 = P4c[i4 - 1];
             if (hp1) xp1 = P4c[i4 + 1];
@@ -468,12 +535,12 @@ __global__ void __launch_bounds__(MAXT, 1)
               dv = ndv;
               uo = nuo;
               if (z + 1 < zeA) {
-                nuo = U4[i4 + PS4];
+                nuo = U4[iu4 + PS4];
                 ndv = __ldg(vrow + (size_t)(z + 1) * VPS4);
               }
             } else {
               dv = __ldg(vrow + (size_t)z * VPS4);
-              uo = U4[i4];
+              uo = U4[iu4];
             }
             const float2 vs01 = mul2(lo(c), inv2), vs23 = mul2(hi(c), inv2);  // v_k
             float2 h01 = mul2(lo(dv), vs01), h23 = mul2(hi(dv), vs23);
@@ -501,7 +568,7 @@ __global__ void __launch_bounds__(MAXT, 1)
             h23.x = in2 ? h23.x : 0.f;
             h23.y = in3 ? h23.y : 0.f;
             const float2 n01 = fma2(ntb2, lo(uo), h01), n23 = fma2(ntb2, hi(uo), h23);
-            U4[i4] = make_float4(n01.x, n01.y, n23.x, n23.y);
+            U4[iu4] = make_float4(n01.x, n01.y, n23.x, n23.y);
             const float2 pa = fma2(vs01, h01, mul2(vs23, h23));
             ka.add(pa.x + pa.y);
           }
@@ -514,7 +581,8 @@ __global__ void __launch_bounds__(MAXT, 1)
         float2 cys[O + 1];
 #pragma unroll
         for (int d = 1; d <= O; d++) cys[d] = splat((ISO ? p.czf[d] : p.cyf[d]) * inv);
-        const int pl4 = zB * PS4 + ql;  // quad index of (x0, y = 0) in plane zB
+        // quad index of (x0, y = 0) in plane zB of P and of U
+        const int pl4 = zB * PS4 + ql + pofs4, pl4u = zB * PS4 + ql + uofs4;
         // ring[j] holds row ybB - 6 + j; row y+7 and U of row y+1 load while row y computes
         float4 ring[W];
 #pragma unroll
@@ -522,16 +590,16 @@ __global__ void __launch_bounds__(MAXT, 1)
           const int yq = ybB - O + j;
           ring[j] = (yq >= 0 && yq < ny) ? P4c[pl4 + yq * nq] : zero4;
         }
-        float4 nuo = U4[pl4 + ybB * nq];
+        float4 nuo = U4[pl4u + ybB * nq];
         for (int y0 = ybB; y0 < yeB; y0 += W) {
 #pragma unroll
           for (int s = 0; s < W; s++) {
             const int y = y0 + s;
             if (y >= yeB) break;
-            const int u4 = pl4 + y * nq;
+            const int u4 = pl4 + y * nq, uu4 = pl4u + y * nq;
             const float4 uo = nuo;
             const float4 nring = y + O + 1 < ny ? P4c[u4 + (O + 1) * nq] : zero4;
-            if (y + 1 < yeB) nuo = U4[u4 + nq];
+            if (y + 1 < yeB) nuo = U4[uu4 + nq];
 #define RING(dd) ring[(s + (dd) + O) % W]
             float2 h01 = make_float2(0.f, 0.f), h23 = make_float2(0.f, 0.f);
 #pragma unroll
@@ -542,7 +610,7 @@ __global__ void __launch_bounds__(MAXT, 1)
             const float4 c = RING(0);
 #undef RING
             const float2 n01 = add2(lo(uo), h01), n23 = add2(hi(uo), h23);
-            U4[u4] = make_float4(n01.x, n01.y, n23.x, n23.y);
+            U4[uu4] = make_float4(n01.x, n01.y, n23.x, n23.y);
             const float2 pa = fma2(mul2(lo(c), inv2), h01, mul2(mul2(hi(c), inv2), h23));
             ka.add(pa.x + pa.y);
             ring[s] = nring;  // row y-6 leaves, row y+7 joins
@@ -562,17 +630,23 @@ __global__ void __launch_bounds__(MAXT, 1)
           const int w1 = (koff[k + 1] - 1) / per;
           for (int w = koff[k] / per; w <= w1; w++) csum += part[(k + w) * NLM + r];
         }
-        const float cv = csum * inv;
-        const float gl = (td.chan_mask & (1 << l)) ? float(td.gamma[l]) : 0.f;
-        const float al = gl * cv;
-        alpha[e] = al;
-        ka.add(al * cv);
+        if constexpr (PAIR) {  // this CTA's part of c, into both CTAs' row cr of cx
+          cx[cr * maxi * NLM + e] = csum;
+          *cooperative_groups::this_cluster().map_shared_rank(cx + cr * maxi * NLM + e, cr ^ 1) = csum;
+        } else {
+          const float cv = csum * inv;
+          const float gl = (td.chan_mask & (1 << l)) ? float(td.gamma[l]) : 0.f;
+          const float al = gl * cv;
+          alpha[e] = al;
+          ka.add(al * cv);
+        }
       }
       {
         const DF ap = df_warp_sum(df_of(ka));
         if (lane == 0) red_a[warp] = make_float2(ap.hi, ap.lo);
       }
-      __syncthreads();
+      if constexpr (PAIR) cooperative_groups::this_cluster().sync();
+      else __syncthreads();
 
       // ---- phase 3: projector scatter U += chi alpha  ||  a_k ----
       {
@@ -580,54 +654,104 @@ __global__ void __launch_bounds__(MAXT, 1)
         while (pos < r_end) {
           const int kend = min(r_end, koff[k + 1]);
           const int shift = pref[k] - koff[k];
-          const float *al = alpha + slot[k] * NLM;
           float coef[NLM];
+          if constexpr (PAIR) {  // alpha = Gamma_l (c_0 + c_1) / b from the two CTAs' rows
+            const int sl = slot[k];
+            const TypeDesc &td = p.types[slot_type[sl]];
 #pragma unroll
-          for (int s = 0; s < NLM; s++) coef[s] = al[s];
-          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStream) {
-            float c[kStream][NLM];
-            unsigned ix[kStream];
+            for (int s = 0; s < NLM; s++) {
+              const int l = p.rank_l[s];
+              const float gl = (td.chan_mask & (1 << l)) ? float(td.gamma[l]) : 0.f;
+              coef[s] = gl * ((cx[sl * NLM + s] + cx[maxi * NLM + sl * NLM + s]) * inv);
+            }
+          } else {
+            const float *al = alpha + slot[k] * NLM;
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
+            for (int s = 0; s < NLM; s++) coef[s] = al[s];
+          }
+          for (int i0 = pos + lane; i0 < kend; i0 += 32 * kStreamS) {
+            float c[kStreamS][NLM];
+            unsigned ix[kStreamS];
+#pragma unroll
+            for (int u = 0; u < kStreamS; u++) {
               const int e = min(i0 + 32 * u, kend - 1) + shift;
               ix[u] = ridx[e];
               Rec::load(rec, e, c[u]);
             }
 #pragma unroll
-            for (int u = 0; u < kStream; u++) {
+            for (int u = 0; u < kStreamS; u++) {
               float val = 0.f;
 #pragma unroll
               for (int s = 0; s < NLM; s++) val = fmaf(c[u][s], coef[s], val);
               // fire-and-forget shared atomics: a plain read-add-write waits on the read
-              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u]], val);
+              if (i0 + 32 * u < kend) atomicAdd(&U[ix[u] - udelta], val);
             }
           }
           pos = kend;
           k++;
         }
       }
-      const DF adf = df_all_reduce(red_a, nw);
-      __syncthreads();
+      DF adf;
+      if constexpr (PAIR) {
+        // <v, V_nl v> = sum Gamma_l c^2 over the slots, the same sum in both CTAs
+        Kahan kn;
+        for (int e = threadIdx.x; e < n_slot * NLM; e += blockDim.x) {
+          const int sl = e / NLM, r = e - sl * NLM;
+          const TypeDesc &td = p.types[slot_type[sl]];
+          const int l = p.rank_l[r];
+          const float gl = (td.chan_mask & (1 << l)) ? float(td.gamma[l]) : 0.f;
+          const float cv = (cx[e] + cx[maxi * NLM + e]) * inv;
+          kn.add(gl * cv * cv);
+        }
+        const DF np = df_warp_sum(df_of(kn));
+        if (lane == 0) red_n[warp] = make_float2(np.hi, np.lo);
+        __syncthreads();
+        // a_k: CTA 0's stencil partials, CTA 1's, then the projector part (fixed order)
+        auto cl = cooperative_groups::this_cluster();
+        const float2 *ra0 = cr == 0 ? red_a : cl.map_shared_rank(red_a, 0);
+        const float2 *ra1 = cr == 1 ? red_a : cl.map_shared_rank(red_a, 1);
+        adf = df_add(df_add(df_all_reduce(ra0, nw), df_all_reduce(ra1, nw)), df_all_reduce(red_n, nw));
+      } else {
+        adf = df_all_reduce(red_a, nw);
+        __syncthreads();
+      }
 
       // ---- phase 4: w = U - a_k v, P <- w, U <- v, b_k^2 partial ----
       {
         const float2 na2 = splat(-(adf.hi + adf.lo));
         Kahan kb;
+        // owned planes: P's at quad e + udelta/4, U's at e.  PAIR: quads [h0, h1) are the
+        // peer's halo planes and also go to its P at e + dpeer.
+        const int nown = nzo * PS4;
+        float4 *P4o = P4 + (udelta >> 2);
+        int h0 = 0, h1 = 0, dpeer = 0;
+        float4 *P4peer = P4;
+        if constexpr (PAIR) {
+          const PairPlanes pq = pair_planes(nz, p.zsplit, cr ^ 1);
+          h0 = (max(zo0, pq.pz0) - zo0) * PS4;
+          h1 = (min(zo1, pq.pz1) - zo0) * PS4;
+          dpeer = (zo0 - pq.pz0) * PS4;
+          P4peer = cooperative_groups::this_cluster().map_shared_rank(P4, cr ^ 1);
+        }
         // the next quad's P and U are read before this quad's are written
         float4 npv = zero4, nuv = zero4;
-        if (threadIdx.x < (nc >> 2)) {
-          npv = P4[threadIdx.x];
+        if (threadIdx.x < nown) {
+          npv = P4o[threadIdx.x];
           nuv = U4[threadIdx.x];
         }
-        for (int e = threadIdx.x; e < (nc >> 2); e += blockDim.x) {
+        for (int e = threadIdx.x; e < nown; e += blockDim.x) {
           const float4 pv = npv, uv = nuv;
-          if (e + (int)blockDim.x < (nc >> 2)) {
-            npv = P4[e + blockDim.x];
+          if (e + (int)blockDim.x < nown) {
+            npv = P4o[e + blockDim.x];
             nuv = U4[e + blockDim.x];
           }
           const float2 v01 = mul2(lo(pv), inv2), v23 = mul2(hi(pv), inv2);
           const float2 w01 = fma2(na2, v01, lo(uv)), w23 = fma2(na2, v23, hi(uv));
-          P4[e] = make_float4(w01.x, w01.y, w23.x, w23.y);
+          const float4 w4 = make_float4(w01.x, w01.y, w23.x, w23.y);
+          P4o[e] = w4;
+          if constexpr (PAIR) {
+            if (e >= h0 && e < h1) P4peer[e + dpeer] = w4;
+          }
           U4[e] = make_float4(v01.x, v01.y, v23.x, v23.y);
           const float2 q = fma2(w01, w01, mul2(w23, w23));
           kb.add(q.x + q.y);
@@ -636,8 +760,17 @@ __global__ void __launch_bounds__(MAXT, 1)
         if (lane == 0) red_b[warp] = make_float2(bp.hi, bp.lo);
         if (threadIdx.x == 0) sab[j] = (double)adf.hi + (double)adf.lo;
       }
-      __syncthreads();
-      const DF b2 = df_all_reduce(red_b, nw);
+      DF b2;
+      if constexpr (PAIR) {  // the halo planes and both CTAs' b partials are in place
+        auto cl = cooperative_groups::this_cluster();
+        cl.sync();
+        const float2 *rb0 = cr == 0 ? red_b : cl.map_shared_rank(red_b, 0);
+        const float2 *rb1 = cr == 1 ? red_b : cl.map_shared_rank(red_b, 1);
+        b2 = df_add(df_all_reduce(rb0, nw), df_all_reduce(rb1, nw));
+      } else {
+        __syncthreads();
+        b2 = df_all_reduce(red_b, nw);
+      }
       const float bf = sqrtf(b2.hi + b2.lo);
       if (threadIdx.x == 0) sab[64 + j] = sqrt((double)b2.hi + (double)b2.lo);
       if (!(bf > 0.f) || !isfinite(bf)) {  // breakdown: the Krylov space is invariant
@@ -653,13 +786,35 @@ __global__ void __launch_bounds__(MAXT, 1)
       tb = bf;
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < p.nqp; r += blockDim.x) {
-      double *o = ab_out + (node - p.node_begin) * 2 * p.nqp;
-      o[r] = sab[r];
-      o[p.nqp + r] = sab[64 + r];
-    }
+    if (cr == 0)
+      for (int r = threadIdx.x; r < p.nqp; r += blockDim.x) {
+        double *o = ab_out + (node - p.node_begin) * 2 * p.nqp;
+        o[r] = sab[r];
+        o[p.nqp + r] = sab[64 + r];
+      }
     __syncthreads();
   }
+  // no CTA of a pair leaves while its peer may still read its shared memory
+  if constexpr (PAIR) cooperative_groups::this_cluster().sync();
+}
+
+template <int MASK, int MAXT, bool ISO>
+__global__ void __launch_bounds__(MAXT, 1)
+    lanczos_quad_kernel(const __grid_constant__ LanczosParams p, const float *__restrict__ veffq,
+                        const ImageMeta *__restrict__ images, const float *__restrict__ tables,
+                        unsigned char *proj_scratch, double *__restrict__ ab_out,
+                        int *__restrict__ status) {
+  quad_body<MASK, MAXT, ISO, false>(p, veffq, images, tables, proj_scratch, ab_out, status);
+}
+
+// One node per cluster of two CTAs (cubes whose P and U do not fit one CTA).
+template <int MASK, bool ISO>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(384, 1)
+    lanczos_quad_pair_kernel(const __grid_constant__ LanczosParams p,
+                             const float *__restrict__ veffq, const ImageMeta *__restrict__ images,
+                             const float *__restrict__ tables, unsigned char *proj_scratch,
+                             double *__restrict__ ab_out, int *__restrict__ status) {
+  quad_body<MASK, 384, ISO, true>(p, veffq, images, tables, proj_scratch, ab_out, status);
 }
 
 template <int MASK, int MAXT, bool ISO>
@@ -673,6 +828,40 @@ cudaError_t launch_quad_variant(const LanczosParams &p, int grid, int block, siz
   k<<<grid, block, smem, s>>>(p, (const float *)veffq, images, (const float *)tables,
                               (unsigned char *)proj_scratch, ab, status);
   return cudaGetLastError();
+}
+
+template <int MASK, bool ISO>
+cudaError_t launch_quad_pair_variant(const LanczosParams &p, int grid, int block, size_t smem,
+                                     cudaStream_t s, const void *veffq, const ImageMeta *images,
+                                     const void *tables, void *proj_scratch, double *ab,
+                                     int *status) {
+  if (block > 384 || grid % 2 != 0) return cudaErrorInvalidConfiguration;
+  auto k = lanczos_quad_pair_kernel<MASK, ISO>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, block, smem, s>>>(p, (const float *)veffq, images, (const float *)tables,
+                              (unsigned char *)proj_scratch, ab, status);
+  return cudaGetLastError();
+}
+
+// Clusters of two that can be resident at once for this block and shared-memory size.
+template <int MASK, bool ISO>
+cudaError_t pair_max_clusters(int block, size_t smem, int *clusters) {
+  auto k = lanczos_quad_pair_kernel<MASK, ISO>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2, 1, 1);
+  cfg.blockDim = dim3(block, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeClusterDimension;
+  attr.val.clusterDim.x = 2;
+  attr.val.clusterDim.y = 1;
+  attr.val.clusterDim.z = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  return cudaOccupancyMaxActiveClusters(clusters, (void *)k, &cfg);
 }
 
 }  // namespace lq

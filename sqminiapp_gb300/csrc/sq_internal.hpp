@@ -67,6 +67,8 @@ struct LanczosParams {
   int ntype;
   int rows_per_warp;       // cube y-rows owned by one warp in the vector passes
   int zchunks;             // kLayoutQuad: z-ranges (pass A) and y-ranges (pass B) per row / plane
+  int ychunks;             // kLayoutPair: y-ranges per plane of pass B (zchunks: z-ranges)
+  int zsplit;              // kLayoutPair: CTA 0 of a pair owns planes [0, zsplit), CTA 1 the rest
   int vq_row;              // kLayoutQuad: row length (floats) of the quad-aligned Veff copies
   long long vq_copy_stride;  // kLayoutQuad: floats per quad-aligned Veff copy
   int proj_cap;            // records of one CTA's projector list (max box points of a node)

@@ -27,6 +27,11 @@ constexpr int kLayoutCompact = 8;
 // over 16-byte quads (lanczos_quad.cuh); rows of 4*ceil(nx/4) floats, no gaps.
 constexpr int kLayoutQuad = 16;
 constexpr int kQuadMaxThreads = 512;
+// With kLayoutQuad, cubes whose P and U do not fit one CTA: a cluster of two CTAs per node,
+// the cube split in z, 6 halo planes of P written by the peer through distributed shared
+// memory (lanczos_quad.cuh, PairPlanes).
+constexpr int kLayoutPair = 32;
+constexpr int kPairThreads = 384;
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;
@@ -57,6 +62,8 @@ cudaError_t launch_veff_extend(const double *veff, double vconst, void *ext, int
 size_t veff_quad_floats(const LanczosParams &p);
 size_t lanczos_quad_smem_bytes(const LanczosParams &p);
 int lanczos_quad_threads(const LanczosParams &p);
+// kLayoutPair: clusters of two CTAs that fit on the device at once (0 if none)
+int lanczos_quad_pair_clusters(const LanczosParams &p, int block, size_t smem);
 
 // Implicit QL of every node's tridiagonal; ab = [n][2][nqp] (a then b).
 cudaError_t launch_quadrature(const double *ab, long long n, int nqp, double *lambda, double *w,

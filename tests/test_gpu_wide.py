@@ -1,8 +1,9 @@
 """GPU parity for the large-cube layouts.
 
 Cubes wider than 32 points: the uneven-batch workload's 32-atom cell (side 17 bohr, 38^3
-mesh, h = 0.4474 bohr, Rcut = 7 bohr, so 33^3 cubes; 40 Lanczos steps) through the FP32 wide
-kernel against the FP64 CPU oracle, and inside a mixed-cell batch.  Cubes of 29^3: FP64 rows
+mesh, h = 0.4474 bohr, Rcut = 7 bohr, so 33^3 cubes; 40 Lanczos steps) through the FP32
+split-pass kernel on CTA pairs and through the single-pass wide kernel, against the FP64 CPU
+oracle, and inside a mixed-cell batch.  Cubes of 29^3: FP64 rows
 without zero columns, FP32 planes without zero rows between them (U on chip).
 
 Tolerance: FP32 vectors (unit roundoff 6e-8) over 40 steps, the same 1e-4 relative bound on
@@ -25,7 +26,10 @@ def _moments(lam, w):
     return [np.sum(w * lam ** k, axis=1) for k in range(4)]
 
 
-def test_wide_cube_matches_oracle(wide_cell, oracle_mod):
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_wide_cube_matches_oracle(wide_cell, oracle_mod, kernel):
+    """kernel 0: the split-pass kernel on a CTA pair per node (U on chip); kernel 1: the
+    single-pass wide kernel (U in global scratch, compact list)."""
     from sqminiapp_gb300 import LSDFT
     d, name, _ = wide_cell
     o = oracle_mod.Oracle(d, name, faithful=False)
@@ -33,11 +37,15 @@ def test_wide_cube_matches_oracle(wide_cell, oracle_mod):
     rng = np.random.default_rng(12)
     veff = -0.25 + 0.05 * rng.standard_normal(o.n_nodes)
     ref = o.nodes_and_weights(nodes=nodes, veff=veff, want_ab=True)
-    with LSDFT(d, name, faithful=False, precision=32) as eng:
+    with LSDFT(d, name, faithful=False, precision=32, kernel=kernel) as eng:
         assert eng.n_nodes == 38 ** 3
-        # y gaps + wide (+ the compact list, which this cell's 33^3 lists need to stay in L2)
-        assert eng.info.kernel_layout & 3 == 3 and eng.info.kernel_u_on_chip == 0
-        assert eng.info.kernel_threads == 576
+        if kernel == 0:
+            assert eng.info.kernel_layout == 16 | 32 and eng.info.kernel_u_on_chip == 1
+            assert eng.info.kernel_threads == 320
+        else:
+            # y gaps + wide (+ the compact list, which this cell's 33^3 lists need in L2)
+            assert eng.info.kernel_layout & 3 == 3 and eng.info.kernel_u_on_chip == 0
+            assert eng.info.kernel_threads == 576
         full = eng.NodesAndWeights_LSSGQ(veff=veff)
         a, b = eng.lanczos_coefficients(eng.n_nodes)
     np.testing.assert_allclose(a[nodes, :3], ref["a"][:, :3], rtol=1e-3, atol=1e-4)
@@ -149,9 +157,11 @@ def _parity(eng_out, ref, nodes, tol):
         assert err < tol, "moment %d error %.3e" % (k, err)
 
 
-def test_fp32_u_in_global_scratch_31cube(tmp_path_factory, oracle_mod):
-    """31^3 cubes (h = 0.5, Rcut = 7.5 bohr): the FP32 kernel keeps P with its y gaps on chip
-    and U in global scratch; FP64 fits no single-CTA layout there."""
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_fp32_31cube(tmp_path_factory, oracle_mod, kernel):
+    """31^3 cubes (h = 0.5, Rcut = 7.5 bohr): the split-pass kernel runs a CTA pair per node
+    (kernel 0); the single-pass kernel (kernel 1) keeps P with its y gaps on chip and U in
+    global scratch; FP64 fits no single-CTA layout there."""
     from sqminiapp_gb300 import LSDFT, SqError
     from sqminiapp_gb300.decks import make_fcc_mg_deck
     d, name, _ = make_fcc_mg_deck(str(tmp_path_factory.mktemp("mg4rc75")), "mg4rc75", ncell=1,
@@ -160,9 +170,12 @@ def test_fp32_u_in_global_scratch_31cube(tmp_path_factory, oracle_mod):
     nodes = np.arange(0, o.n_nodes, 131)
     veff = np.full(o.n_nodes, -0.2)
     ref = o.nodes_and_weights(nodes=nodes, veff=veff)
-    with LSDFT(d, name, faithful=False, precision=32) as eng:
+    with LSDFT(d, name, faithful=False, precision=32, kernel=kernel) as eng:
         assert eng.cube == (31, 31, 31)
-        assert eng.info.kernel_layout & 7 == 1 and eng.info.kernel_u_on_chip == 0
+        if kernel == 0:
+            assert eng.info.kernel_layout == 16 | 32 and eng.info.kernel_u_on_chip == 1
+        else:
+            assert eng.info.kernel_layout & 7 == 1 and eng.info.kernel_u_on_chip == 0
         got = eng.NodesAndWeights_LSSGQ(veff=veff)
     _parity(got, ref, nodes, 1e-4)
     with pytest.raises(SqError) as e:

@@ -6,7 +6,7 @@ import pytest
 from sqminiapp_gb300 import GB300_DEVICE, SqError, plan_kernel
 from sqminiapp_gb300.decks import CONFIGS, make_fcc_mg_deck
 
-YGAP, WIDE, XCLAMP, COMPACT, QUAD = 1, 2, 4, 8, 16
+YGAP, WIDE, XCLAMP, COMPACT, QUAD, PAIR = 1, 2, 4, 8, 16, 32
 
 
 @pytest.fixture(scope="module")
@@ -33,8 +33,10 @@ def test_fp32_layouts(decks):
     assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (QUAD, 1, 352)
     p = _plan(decks, "mg500_h0.5_rc7_q50")  # 29^3: 8 quads x 29 x 2 = 464 -> 480
     assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (QUAD, 1, 480)
-    p = _plan(decks, "uneven_b_mg32_h0.45_rc7_q40")  # 33^3: wide, U in L2, compact list
-    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP | WIDE | COMPACT, 0, 576)
+    # 33^3: a pair of CTAs per node, each with half the planes (9 quads x 33 rows, one z-range;
+    # 17 planes x 9 quads x 2 y-ranges = 306 -> 320 threads), U on chip
+    p = _plan(decks, "uneven_b_mg32_h0.45_rc7_q40")
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (QUAD | PAIR, 1, 320)
     for name in decks:
         assert 0 < _plan(decks, name).kernel_smem_bytes <= smem_max
 
@@ -46,6 +48,8 @@ def test_single_pass_kernel_layouts(decks):
     assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 1)
     p = _plan(decks, "mg500_h0.5_rc7_q50", kernel=1)  # 29^3: U on chip only without the y gaps
     assert (p.kernel_layout, p.kernel_u_on_chip) == (0, 1)
+    p = _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", kernel=1)  # 33^3: wide, U in L2, compact
+    assert (p.kernel_layout, p.kernel_u_on_chip, p.kernel_threads) == (YGAP | WIDE | COMPACT, 0, 576)
 
 
 def test_kernel_option(decks):
@@ -55,8 +59,9 @@ def test_kernel_option(decks):
     for kw in ({"faithful": True}, {"precision": 64}, {"list_format": 2}):
         with pytest.raises(SqError):
             _plan(decks, "mg32_h0.5_rc6.5_q40", kernel=2, **kw)
-    with pytest.raises(SqError):
-        _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", kernel=2)  # 33 points wide
+    assert _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", kernel=2).kernel_layout == QUAD | PAIR
+    with pytest.raises(SqError):  # the pair runs one tile only
+        _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", kernel=2, tile=1)
     with pytest.raises(SqError):
         _plan(decks, "mg32_h0.5_rc6.5_q40", kernel=3)
     # a tile whose threads exceed the kernel's 512 falls back to the single-pass kernel
@@ -64,7 +69,9 @@ def test_kernel_option(decks):
 
 
 def test_list_format_option(decks):
-    assert _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", list_format=1).kernel_layout == YGAP | WIDE
+    assert _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", list_format=1).kernel_layout == QUAD | PAIR
+    assert _plan(decks, "uneven_b_mg32_h0.45_rc7_q40", list_format=1,
+                 kernel=1).kernel_layout == YGAP | WIDE
     assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=2).kernel_layout == YGAP | COMPACT
     assert _plan(decks, "mg32_h0.5_rc6.5_q40", list_format=1).kernel_layout == QUAD
     # the faithful operator and FP64 keep the full records
@@ -88,7 +95,11 @@ def test_fp64_layouts(decks):
 
 
 def test_smaller_shared_memory_moves_u_off_chip(decks):
+    # the split-pass kernel moves to a CTA pair per node; the single-pass one keeps P on chip
+    # and moves U to global scratch
     p = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 160 * 1024})
+    assert (p.kernel_layout, p.kernel_u_on_chip) == (QUAD | PAIR, 1)
+    p = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 160 * 1024}, kernel=1)
     assert (p.kernel_layout, p.kernel_u_on_chip) == (YGAP, 0)
     p = _plan(decks, "mg32_h0.5_rc6.5_q40", device={"smem_optin": 170 * 1024})
     assert (p.kernel_layout, p.kernel_u_on_chip) == (QUAD, 1)
