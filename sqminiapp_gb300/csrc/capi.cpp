@@ -350,7 +350,9 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
         p = q;
         h->quad = true;
         h->u_smem = true;
-        h->block = pt;
+        // all 12 warps of the register budget: the stencil passes use pt threads, the list
+        // streams and the update all of them (fewer, longer warp ranges are slower)
+        h->block = sq::kPairThreads;
         h->tuned = true;  // one tile
       }
     }

@@ -41,7 +41,7 @@ def test_wide_cube_matches_oracle(wide_cell, oracle_mod, kernel):
         assert eng.n_nodes == 38 ** 3
         if kernel == 0:
             assert eng.info.kernel_layout == 16 | 32 and eng.info.kernel_u_on_chip == 1
-            assert eng.info.kernel_threads == 320
+            assert eng.info.kernel_threads == 384
         else:
             # y gaps + wide (+ the compact list, which this cell's 33^3 lists need in L2)
             assert eng.info.kernel_layout & 3 == 3 and eng.info.kernel_u_on_chip == 0
