@@ -332,7 +332,7 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
       p = q;
       h->quad = true;
       h->u_smem = true;
-      h->block = threads;
+      h->block = sq::lanczos_quad_block(q);
     } else if (h->opt.tile == 0 && p.nz >= 2 * sq::kStencilHalf + 2) {
       // the same kernel on a pair of CTAs per node, the cube split in z: each holds its half
       // of U and its half of P plus 6 halo planes; each streams its half of the list
@@ -555,7 +555,8 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
       float ms = 0.f;
       for (int rep = 0; rep < 2; rep++) {  // the first launch of a tile loads its code
         ck(cudaEventRecord(t0, s), "event");
-        ck(sq::launch_lanczos(q, 32, false, true, grid, threads, h->smem, s, h->d_veff_ext,
+        ck(sq::launch_lanczos(q, 32, false, true, grid, sq::lanczos_quad_block(q), h->smem, s,
+                              h->d_veff_ext,
                               h->d_images, h->d_tables, h->d_u, h->d_proj, h->d_ab, h->d_status),
            "lanczos (tile probe)");
         ck(cudaEventRecord(t1, s), "event");
@@ -570,7 +571,7 @@ sq_status run_device(sq_handle *h, const double *d_veff, double veff_const, long
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     h->lp.zchunks = p.zchunks = best_tile;
-    h->block = sq::lanczos_quad_threads(p);
+    h->block = sq::lanczos_quad_block(p);
     h->info.kernel_threads = h->block;
     h->tuned = true;
   }

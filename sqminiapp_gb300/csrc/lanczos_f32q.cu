@@ -14,6 +14,14 @@ int lanczos_quad_threads(const LanczosParams &p) {
   return std::max(64, 32 * (((p.pitch / 4) * groups + 31) / 32));
 }
 
+int lanczos_quad_block(const LanczosParams &p) {
+  // every warp of the register budget (12 warps at up to 384 threads, 16 above): the passes
+  // use lanczos_quad_threads of them, the list streams and the update all
+  const int t = lanczos_quad_threads(p);
+  if (t <= 256) return t;
+  return t <= 384 ? 384 : kQuadMaxThreads;
+}
+
 size_t lanczos_quad_smem_bytes(const LanczosParams &p) {
   const bool pair = (p.layout & kLayoutPair) != 0;
   const size_t ps = lq::quad_plane_floats(p.ny, p.pitch);

@@ -62,6 +62,8 @@ cudaError_t launch_veff_extend(const double *veff, double vconst, void *ext, int
 size_t veff_quad_floats(const LanczosParams &p);
 size_t lanczos_quad_smem_bytes(const LanczosParams &p);
 int lanczos_quad_threads(const LanczosParams &p);
+// threads to launch a single-CTA split-pass kernel with (>= lanczos_quad_threads)
+int lanczos_quad_block(const LanczosParams &p);
 // kLayoutPair: clusters of two CTAs that fit on the device at once (0 if none)
 int lanczos_quad_pair_clusters(const LanczosParams &p, int block, size_t smem);
 

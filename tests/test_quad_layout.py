@@ -30,27 +30,36 @@ def quad_threads(n, tile):
     return max(64, 32 * ((nq * n * tile + 31) // 32))
 
 
+def quad_block(n, tile):
+    """Threads the engine launches: the passes' threads, rounded up to every warp of the
+    register budget (12 warps up to 384 threads, 16 above) once they pass 256."""
+    t = quad_threads(n, tile)
+    return t if t <= 256 else (384 if t <= 384 else 512)
+
+
 @pytest.mark.parametrize("n,h", [(3, 0.85), (5, 0.85), (9, 0.85), (17, 0.5), (27, 0.5)])
 @pytest.mark.parametrize("tile", [1, 2, 3, 4])
 def test_engine_thread_count(n, h, tile, tmp_path):
     """The engine's thread count for a tile (sq_plan_kernel) is the restated one, and always
-    at least two warps: warp 0 builds a node's image list while the others clear P and U."""
+    at least two warps: warp 0 builds a node's image list while the others clear P and U.
+    Above 256 threads the launch takes every warp of the register budget."""
     from sqminiapp_gb300 import plan_kernel
     from sqminiapp_gb300.decks import make_fcc_mg_deck
     rcut = h * (n - 1) / 2
     d, name, _ = make_fcc_mg_deck(str(tmp_path), "c", ncell=1, h=h, rcut=rcut, n_qp=8)
-    want = quad_threads(n, tile)
-    if want > MAX_THREADS:
+    if quad_threads(n, tile) > MAX_THREADS:
         return
     p = plan_kernel(d, name, kernel=2, tile=tile)
     assert p.cube[0] == n
-    assert p.kernel_threads == want >= 64
+    assert p.kernel_threads == quad_block(n, tile) >= quad_threads(n, tile) >= 64
 
 
 def thread_maps(n, tile):
     """Per thread: pass-A (y, quad, zb, ze, active) and pass-B (z, quad, yb, ye, active)."""
     nq = (n + 3) // 4
-    t = np.arange(quad_threads(n, tile))
+    # the launch's threads (those past the passes' need stay idle); the algebra test also
+    # runs tiles above the kernel's 512 threads, with exactly the threads they need
+    t = np.arange(max(quad_threads(n, tile), quad_block(n, tile)))
     grp, ql = t // nq, t % nq
     ln = (n + tile - 1) // tile
     yA, zc = grp % n, grp // n
