@@ -310,6 +310,7 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
   p.zchunks = 1;
   p.ychunks = 1;
   p.zsplit = 0;
+  p.vring = 0;
   p.vq_row = 4 * ((p.EX + 6 + 3) / 4);  // the row of a quad-aligned Veff copy (see below)
   p.vq_copy_stride = (long long)p.vq_row * p.EY * p.EZ;
   h->quad = false;
@@ -333,6 +334,9 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
       h->quad = true;
       h->u_smem = true;
       h->block = sq::lanczos_quad_block(q);
+      p.vring = 1;  // pass A's Veff rings, where they fit (12-warp budget only)
+      if (h->block > sq::kVRingThreads || sq::lanczos_quad_smem_bytes(p) > (size_t)smem_optin)
+        p.vring = 0;
     } else if (h->opt.tile == 0 && p.nz >= 2 * sq::kStencilHalf + 2) {
       // the same kernel on a pair of CTAs per node, the cube split in z: each holds its half
       // of U and its half of P plus 6 halo planes; each streams its half of the list
@@ -348,6 +352,8 @@ void plan_engine(sq_handle *h, int smem_optin, int l2_bytes) {
       if (pt <= sq::kPairThreads && sq::lanczos_quad_smem_bytes(q) <= (size_t)smem_optin &&
           (h->opt.list_format == 1 || 0.5 * list_bytes <= 0.75 * (double)l2_bytes)) {
         p = q;
+        p.vring = 1;
+        if (sq::lanczos_quad_smem_bytes(p) > (size_t)smem_optin) p.vring = 0;
         h->quad = true;
         h->u_smem = true;
         // all 12 warps of the register budget: the stencil passes use pt threads, the list

@@ -35,6 +35,7 @@ size_t lanczos_quad_smem_bytes(const LanczosParams &p) {
     b += sizeof(float) * 2 * (size_t)p.max_img * nlm + 8 + sizeof(float) * 2 * lk::kMaxWarps +
          sizeof(int) * 4;
   b += sizeof(int) * (9 * (size_t)p.max_img + 2) + sizeof(int) * 4;    // per-node image lists
+  if (p.vring) b += 16 + sizeof(float) * 4 * kVRingSlots * kVRingThreads;  // Veff rings
   return b;
 }
 

@@ -225,6 +225,9 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
   int *koff = kept + maxi;      // maxi + 1
   int *slot_first = koff + maxi + 1;  // first image of every slot (images sorted by atom)
   int *cnt = slot_first + maxi;  // [0] images, [1] slots, [2] overflow, [3] next node
+  // per-thread Veff rings of pass A (p.vring): kVRingSlots float4 per thread, 16-byte aligned
+  float4 *vring = reinterpret_cast<float4 *>(
+      (reinterpret_cast<uintptr_t>(cnt + 4) + 15) & ~static_cast<uintptr_t>(15));
 
   typename Rec::vec_t *rec = reinterpret_cast<typename Rec::vec_t *>(
       proj_scratch + (size_t)blockIdx.x * p.proj_bytes_per_cta);
@@ -508,13 +511,28 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
         float2 xm2 = make_float2(0.f, 0.f), xp2 = make_float2(0.f, 0.f);
         float4 xm1 = zero4, xp1 = zero4;
         const float2 *P2c = reinterpret_cast<const float2 *>(P);
-        // U and Veff of plane z+1 load while plane z is computed (in the 12-warp budget; the
-        // 16-warp one has no registers to spare for it)
+        // U of plane z+1 loads while plane z is computed, and Veff (from L2) kVRingSlots - 1
+        // planes ahead through the thread's ring of async copies (p.vring; else one plane
+        // ahead in registers).  The 16-warp budget has no registers to spare for either.
         constexpr bool kPrefetch = MAXT <= 384;
+        constexpr int kAhead = kVRingSlots - 1;
+        const bool use_ring = kPrefetch && p.vring;
+        const unsigned vr0 = (unsigned)__cvta_generic_to_shared(vring + threadIdx.x * kVRingSlots);
+        auto vcopy = [&](int zc, int slot) {  // Veff quad of plane zc into ring slot
+          if (zc < zeA)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(vr0 + 16u * slot),
+                         "l"(__cvta_generic_to_global(vrow + (size_t)zc * VPS4))
+                         : "memory");
+          asm volatile("cp.async.commit_group;" ::: "memory");  // one group per plane, even empty
+        };
         float4 nuo = zero4, ndv = zero4;
         if constexpr (kPrefetch) {
           nuo = U4[row4 + zbA * PS4 + uofs4];
-          ndv = __ldg(vrow + (size_t)zbA * VPS4);
+          if (use_ring) {
+            for (int d = 0; d < kAhead; d++) vcopy(zbA + d, d);
+          } else {
+            ndv = __ldg(vrow + (size_t)zbA * VPS4);
+          }
         }
         for (int z0 = zbA; z0 < zeA; z0 += W) {
 #pragma unroll
@@ -532,12 +550,19 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
             const float4 c = RING(0);
             float4 dv, uo;
             if constexpr (kPrefetch) {
-              dv = ndv;
-              uo = nuo;
-              if (z + 1 < zeA) {
-                nuo = U4[iu4 + PS4];
-                ndv = __ldg(vrow + (size_t)(z + 1) * VPS4);
+              if (use_ring) {
+                // plane z's copy is done once at most kAhead - 1 later groups are pending; the
+                // copy of plane z + kAhead then goes to the slot read one plane earlier
+                asm volatile("cp.async.wait_group %0;" ::"n"(kAhead - 1) : "memory");
+                const int i = z - zbA;
+                dv = vring[threadIdx.x * kVRingSlots + (i & (kVRingSlots - 1))];
+                vcopy(z + kAhead, (i + kAhead) & (kVRingSlots - 1));
+              } else {
+                dv = ndv;
+                if (z + 1 < zeA) ndv = __ldg(vrow + (size_t)(z + 1) * VPS4);
               }
+              uo = nuo;
+              if (z + 1 < zeA) nuo = U4[iu4 + PS4];
             } else {
               dv = __ldg(vrow + (size_t)z * VPS4);
               uo = U4[iu4];

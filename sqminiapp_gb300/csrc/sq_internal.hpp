@@ -69,6 +69,7 @@ struct LanczosParams {
   int zchunks;             // kLayoutQuad: z-ranges (pass A) and y-ranges (pass B) per row / plane
   int ychunks;             // kLayoutPair: y-ranges per plane of pass B (zchunks: z-ranges)
   int zsplit;              // kLayoutPair: CTA 0 of a pair owns planes [0, zsplit), CTA 1 the rest
+  int vring;               // kLayoutQuad: 1 = pass A stages Veff through a per-thread shared ring
   int vq_row;              // kLayoutQuad: row length (floats) of the quad-aligned Veff copies
   long long vq_copy_stride;  // kLayoutQuad: floats per quad-aligned Veff copy
   int proj_cap;            // records of one CTA's projector list (max box points of a node)

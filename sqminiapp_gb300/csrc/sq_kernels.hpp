@@ -32,6 +32,10 @@ constexpr int kQuadMaxThreads = 512;
 // memory (lanczos_quad.cuh, PairPlanes).
 constexpr int kLayoutPair = 32;
 constexpr int kPairThreads = 384;
+// Pass A of the split-pass kernel (12-warp budget) stages Veff through a per-thread ring of
+// kVRingSlots float4 in shared memory, filled by async copies kVRingSlots - 1 planes ahead.
+constexpr int kVRingSlots = 4;
+constexpr int kVRingThreads = 384;
 
 // device status bits (ORed by the kernels)
 constexpr int kStatusCapacity = 1;
