@@ -313,3 +313,41 @@ def test_float4_accesses_are_bank_conflict_free(n, tile):
     check(zb * ps + yA * pitch + 4 * ql, actA, zb)
     # y pass, every thread at the same offset into its y-range
     check(zB * ps + yb * pitch + 4 * ql, actB, yb)
+
+
+@pytest.mark.parametrize("planes", list(range(1, 30)))
+def test_veff_ring_slots_and_groups(planes):
+    """Pass A's Veff ring (lanczos_quad.cuh, kVRingSlots = 4, three planes ahead), restated:
+    the prologue commits one group per plane 0..2 (empty past the range), every plane waits
+    until at most 2 groups are pending, reads its slot and commits the copy of plane + 3 into
+    the slot read one plane earlier.  Every read finds its own plane's copy complete, and no
+    copy overwrites a slot before its plane has been read."""
+    slots, ahead = 4, 3
+    ring = [None] * slots
+    groups = []  # (plane or None, slot)
+    done = 0     # groups completed so far (in order)
+
+    assigned = [None] * slots  # the plane last issued into each slot
+
+    def commit(plane, slot):
+        if plane < planes:
+            # the copy may land at once: the slot's previous plane must already have been read
+            assert assigned[slot] is None or assigned[slot] in read, "slot reused early"
+            assigned[slot] = plane
+        groups.append((plane if plane < planes else None, slot))
+
+    read = set()
+    for d in range(ahead):
+        commit(d, d)
+    for i in range(planes):
+        # cp.async.wait_group 2: complete the oldest groups until at most 2 are pending
+        while len(groups) - done > ahead - 1:
+            plane, slot = groups[done]
+            if plane is not None:
+                assert ring[slot] is None or ring[slot] in read, "slot overwritten unread"
+                ring[slot] = plane
+            done += 1
+        assert ring[i & (slots - 1)] == i
+        read.add(i)
+        commit(i + ahead, (i + ahead) & (slots - 1))
+    assert read == set(range(planes))
