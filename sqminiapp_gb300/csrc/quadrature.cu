@@ -7,7 +7,10 @@
 // results identical to the full-matrix form.
 //
 // One thread per node, FP64.  This file is compiled with -fmad=false so every operation is
-// a separately rounded IEEE multiply or add, the same arithmetic as the CPU reference.
+// a separately rounded IEEE multiply or add, the same arithmetic as the CPU reference.  The
+// three working arrays of a node (d, e and row 0 of Z, N_qp doubles each) live in shared
+// memory, one column per thread (element i of thread t at i * blockDim + t): as local arrays
+// the ~250 nodes per SM (1.5 KB each) overflow L1 and every rotation waits on L2.
 #include <cuda_runtime.h>
 
 #include "sq_kernels.hpp"
@@ -16,15 +19,26 @@ namespace sq {
 
 namespace {
 
-constexpr int kMaxQp = 64;
+constexpr int kQuadBlock = 64;
 
-__global__ void quadrature_kernel(const double *__restrict__ ab, long long n, int nqp,
-                                  double *__restrict__ lambda, double *__restrict__ wts,
-                                  double *__restrict__ lmin, double *__restrict__ lmax,
-                                  int *__restrict__ status) {
+// one thread's column of a shared array: element i at p[i * stride]
+struct Col {
+  double *p;
+  int stride;
+  __device__ __forceinline__ double &operator[](int i) const { return p[i * stride]; }
+};
+
+__global__ void __launch_bounds__(kQuadBlock)
+    quadrature_kernel(const double *__restrict__ ab, long long n, int nqp,
+                      double *__restrict__ lambda, double *__restrict__ wts,
+                      double *__restrict__ lmin, double *__restrict__ lmax,
+                      int *__restrict__ status) {
+  extern __shared__ double qsm[];  // [3][nqp][blockDim]
+  const Col d{qsm + threadIdx.x, (int)blockDim.x};
+  const Col e{qsm + nqp * blockDim.x + threadIdx.x, (int)blockDim.x};
+  const Col z{qsm + 2 * nqp * blockDim.x + threadIdx.x, (int)blockDim.x};
   for (long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x; node < n;
        node += (long long)gridDim.x * blockDim.x) {
-    double d[kMaxQp], e[kMaxQp], z[kMaxQp];
     const double *a = ab + node * 2 * nqp;
     const double *b = a + nqp;
     for (int i = 0; i < nqp; i++) {
@@ -96,10 +110,15 @@ __global__ void quadrature_kernel(const double *__restrict__ ab, long long n, in
 cudaError_t launch_quadrature(const double *ab, long long n, int nqp, double *lambda, double *w,
                               double *lmin, double *lmax, int *status, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  const int block = 128;
+  if (nqp < 1 || nqp > 64) return cudaErrorInvalidValue;
+  const int block = kQuadBlock;
+  const size_t smem = sizeof(double) * 3 * (size_t)nqp * block;
+  cudaError_t e = cudaFuncSetAttribute(quadrature_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   const long long blocks = (n + block - 1) / block;
-  const int grid = (int)(blocks < 152LL * 32 ? blocks : 152LL * 32);
-  quadrature_kernel<<<grid, block, 0, s>>>(ab, n, nqp, lambda, w, lmin, lmax, status);
+  const int grid = (int)(blocks < 152LL * 64 ? blocks : 152LL * 64);
+  quadrature_kernel<<<grid, block, smem, s>>>(ab, n, nqp, lambda, w, lmin, lmax, status);
   return cudaGetLastError();
 }
 
