@@ -225,7 +225,8 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
   int *koff = kept + maxi;      // maxi + 1
   int *slot_first = koff + maxi + 1;  // first image of every slot (images sorted by atom)
   int *cnt = slot_first + maxi;  // [0] images, [1] slots, [2] overflow, [3] next node
-  // per-thread Veff rings of pass A (p.vring): kVRingSlots float4 per thread, 16-byte aligned
+  // Veff rings of pass A (p.vring): slot s of thread t at s * kVRingThreads + t, so a warp's
+  // accesses to one slot are 512 contiguous bytes (no bank conflicts); 16-byte aligned
   float4 *vring = reinterpret_cast<float4 *>(
       (reinterpret_cast<uintptr_t>(cnt + 4) + 15) & ~static_cast<uintptr_t>(15));
 
@@ -517,10 +518,11 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
         constexpr bool kPrefetch = MAXT <= 384;
         constexpr int kAhead = kVRingSlots - 1;
         const bool use_ring = kPrefetch && p.vring;
-        const unsigned vr0 = (unsigned)__cvta_generic_to_shared(vring + threadIdx.x * kVRingSlots);
+        const unsigned vr0 = (unsigned)__cvta_generic_to_shared(vring + threadIdx.x);
         auto vcopy = [&](int zc, int slot) {  // Veff quad of plane zc into ring slot
           if (zc < zeA)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(vr0 + 16u * slot),
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(
+                             vr0 + 16u * (unsigned)(slot * kVRingThreads)),
                          "l"(__cvta_generic_to_global(vrow + (size_t)zc * VPS4))
                          : "memory");
           asm volatile("cp.async.commit_group;" ::: "memory");  // one group per plane, even empty
@@ -555,7 +557,7 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
                 // copy of plane z + kAhead then goes to the slot read one plane earlier
                 asm volatile("cp.async.wait_group %0;" ::"n"(kAhead - 1) : "memory");
                 const int i = z - zbA;
-                dv = vring[threadIdx.x * kVRingSlots + (i & (kVRingSlots - 1))];
+                dv = vring[(i & (kVRingSlots - 1)) * kVRingThreads + threadIdx.x];
                 vcopy(z + kAhead, (i + kAhead) & (kVRingSlots - 1));
               } else {
                 dv = ndv;
