@@ -81,6 +81,9 @@ def parse_args():
     p.add_argument("--scf-model", default=WARM_START_MODEL,
                    help="learned start for the FP32 engine ('none' skips it); used when the cell "
                         "has the discretisation the model was trained at")
+    p.add_argument("--scf-learned-highpass", type=float, default=0.0,
+                   help="learned start: keep the network's correction above this wave vector "
+                        "(k^2/(k^2+k0^2), 1/bohr); 0 keeps all of it")
     p.add_argument("--scf-learned", choices=["auto", "force"], default="auto",
                    help="force: run the learned start on a cell of another discretisation too")
     p.add_argument("--scf-fp64", choices=["full", "at-fp32-density"], default="full",
@@ -473,7 +476,7 @@ RES_STOP = 3e-5   # relative density residual, the FP32 engine's floor-safe tole
 DF_STOP = 1e-5    # |F_k - F_(k-1)| per atom (Ha), the benchmark spec's energy tolerance
 
 
-def _scf_trace(eng, mixing, tol, model=None, maxit=100):
+def _scf_trace(eng, mixing, tol, model=None, maxit=100, highpass=0.0):
     """One SCF from the atomic superposition (or the learned start), stepped by hand so every
     iteration's host wall time, free energy per atom, residual and Fermi level are recorded.
     The clock starts before the start density is formed (the learned start's descriptors
@@ -482,7 +485,7 @@ def _scf_trace(eng, mixing, tol, model=None, maxit=100):
     t0 = time.perf_counter()
     if model is not None:
         opt = eng._scf_options(tol, None, mixing.get("mixing_parameter"), None, None, None,
-                               mixing.get("kerker_ktf"))
+                               mixing.get("kerker_ktf"), learned_highpass=highpass)
         import ctypes
         from sqminiapp_gb300.capi import check
         check(eng._lib.sq_scf_begin_learned(eng._h, ctypes.byref(opt), model._m),
@@ -565,8 +568,9 @@ def scf_leg(args, local):
         from sqminiapp_gb300 import WarmStartMLP
         model = WarmStartMLP(device=local, path=args.scf_model)
         eng = LSDFT(deck_dir, name, faithful=False, precision=32, device=local)
-        tr = _scf_trace(eng, mixing, None, model=model)
+        tr = _scf_trace(eng, mixing, None, model=model, highpass=args.scf_learned_highpass)
         tr["model"] = os.path.basename(args.scf_model)
+        tr["learned_highpass_k0"] = args.scf_learned_highpass
         out["fp32_learned"] = tr
         rho["32L"] = eng.scf_density()[0].copy()
         eng.close()

@@ -305,6 +305,10 @@ typedef struct sq_scf_options {
   int cuda_graph;           /* 1: from the second iteration on, replay one captured CUDA graph
                                of the iteration's device part (Poisson, potential, Lanczos,
                                quadrature); 0: direct launches */
+  double learned_highpass;  /* sq_scf_begin_learned only: > 0 keeps of the network's correction
+                               to the atomic superposition only its short wavelengths, scaled
+                               by k^2 / (k^2 + k0^2) with k0 this value (1/bohr); 0 the whole
+                               correction */
 } sq_scf_options;
 
 typedef struct sq_scf_result {

@@ -216,15 +216,15 @@ class LSDFT:
     # --- SCF closure (SCF_LSSGQ, src/lsdft.h:153) -----------------------------------------
     @staticmethod
     def _scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency, fermi_tol,
-                     kerker_ktf=None, cuda_graph=False):
+                     kerker_ktf=None, cuda_graph=False, learned_highpass=None):
         return SqScfOptions(float(tol or 0.0), int(maxit or 0), float(mixing_parameter or 0.0),
                             int(mixing_history or 0), int(pulay_frequency or 0),
                             float(fermi_tol or 0.0), float(kerker_ktf or 0.0),
-                            int(bool(cuda_graph)))
+                            int(bool(cuda_graph)), float(learned_highpass or 0.0))
 
     def SCF_LSSGQ(self, rho_init=None, tol=None, maxit=None, mixing_parameter=None,
                   mixing_history=None, pulay_frequency=None, fermi_tol=None, kerker_ktf=None,
-                  raise_on_maxit=True, model=None, cuda_graph=False):
+                  raise_on_maxit=True, model=None, cuda_graph=False, learned_highpass=None):
         """Self-consistent field loop on the GPU until ||rho_out - rho_in|| / ||rho_out|| < tol.
 
         rho_init: None (superposition of atomic valence densities) or a host density over the
@@ -233,7 +233,7 @@ class LSDFT:
         k_TF = 1/bohr, negative = unpreconditioned mixing.  Returns the result dict of the
         last iteration with the per-iteration history of free energy and residual."""
         opt = self._scf_options(tol, maxit, mixing_parameter, mixing_history, pulay_frequency,
-                                fermi_tol, kerker_ktf, cuda_graph)
+                                fermi_tol, kerker_ktf, cuda_graph, learned_highpass)
         if model is not None:
             # learned start (sq_scf_begin_learned), then the same loop one step at a time
             check(self._lib.sq_scf_begin_learned(self._h, ctypes.byref(opt), model._m),

@@ -64,7 +64,8 @@ class SqScfOptions(ctypes.Structure):
     _fields_ = [("tol", ctypes.c_double), ("maxit", ctypes.c_int),
                 ("mixing_parameter", ctypes.c_double), ("mixing_history", ctypes.c_int),
                 ("pulay_frequency", ctypes.c_int), ("fermi_tol", ctypes.c_double),
-                ("kerker_ktf", ctypes.c_double), ("cuda_graph", ctypes.c_int)]
+                ("kerker_ktf", ctypes.c_double), ("cuda_graph", ctypes.c_int),
+                ("learned_highpass", ctypes.c_double)]
 
 
 class SqScfResult(ctypes.Structure):

@@ -40,6 +40,7 @@ namespace sq {
 double *scf_rho0_device(sq_handle *h);
 double *scf_rho_out_device(sq_handle *h);
 void scf_begin_device_density(sq_handle *h, const sq_scf_options *o, const double *d_rho);
+void scf_highpass_start(sq_handle *h, double k0);
 
 namespace {
 
@@ -1108,7 +1109,10 @@ sq_status sq_scf_begin_learned(sq_handle *h, const sq_scf_options *opt, sq_mlp *
                                                              m->t_std, n, rho_d.get());
     ck_launch("correction");
     sq_status st = mlp_status(m);
-    if (st == SQ_OK) scf_begin_device_density(h, opt, rho_d.get());  // copies rho; synchronises
+    if (st == SQ_OK) {
+      scf_begin_device_density(h, opt, rho_d.get());  // copies rho; synchronises
+      if (opt && opt->learned_highpass > 0.0) scf_highpass_start(h, opt->learned_highpass);
+    }
     return st;
   });
 }

@@ -243,6 +243,13 @@ __global__ void kerker_kernel(cufftDoubleComplex *__restrict__ spec, const doubl
   }
 }
 
+__global__ void sub_kernel(const double *__restrict__ a, const double *__restrict__ b,
+                           double *__restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = a[i] - b[i];
+}
+
 // x = max(0, x + beta w) (w may alias nothing else); partial sums of the new x.
 __global__ void __launch_bounds__(kBlock)
     mix_kernel(double *__restrict__ x, const double *__restrict__ w, double beta, long long n,
@@ -633,6 +640,33 @@ double *scf_rho0_device(sq_handle *h) { return scf_state(h).d_rho0; }
 double *scf_rho_out_device(sq_handle *h) { return scf_state(h).d_rho_out; }
 void scf_begin_device_density(sq_handle *h, const sq_scf_options *o, const double *d_rho) {
   begin(h, o, d_rho, true, h->own_stream);
+}
+
+// After a learned start: keep of its correction to the atomic superposition only the short
+// wavelengths, rho_in = max(0, rho0 + P (rho_in - rho0)) with the Kerker symbol
+// P = k^2 / (k^2 + k0^2), scaled to the electron count.  A local model's error at long
+// wavelengths is the part a metal's density response amplifies (as 1/k^2).
+void scf_highpass_start(sq_handle *h, double k0) {
+  ScfState &s = *h->scf;
+  const cudaStream_t st = h->own_stream;
+  sub_kernel<<<grid_for(s.ng), kBlock, 0, st>>>(s.d_rho_in, s.d_rho0, s.d_work, s.ng);
+  ck(cudaGetLastError(), "correction");
+  ckfft(cufftSetStream(s.plan_f, st), "fft stream");
+  ckfft(cufftSetStream(s.plan_i, st), "fft stream");
+  ckfft(cufftExecD2Z(s.plan_f, s.d_work, s.d_spec), "D2Z");
+  kerker_kernel<<<grid_for(s.nspec), kBlock, 0, st>>>(s.d_spec, s.d_green, s.nspec, k0 * k0,
+                                                      1.0 / (double)s.ng);
+  ck(cudaGetLastError(), "high-pass");
+  ckfft(cufftExecZ2D(s.plan_i, s.d_spec, s.d_work), "Z2D");
+  ck(cudaMemcpyAsync(s.d_rho_in, s.d_rho0, sizeof(double) * (size_t)s.ng,
+                     cudaMemcpyDeviceToDevice, st), "rho0 copy");
+  mix_kernel<<<kRedBlocks, kBlock, 0, st>>>(s.d_rho_in, s.d_work, 1.0, s.ng, s.d_part);
+  ck(cudaGetLastError(), "start");
+  finish_sums<<<1, 256, 0, st>>>(s.d_part, kRedBlocks, 1, s.d_sums);
+  scale_kernel<<<grid_for(s.ng), kBlock, 0, st>>>(s.d_rho_in, s.d_sums,
+                                                  h->deck.n_electrons / h->setup.dV, s.ng);
+  ck(cudaGetLastError(), "scale");
+  ck(cudaStreamSynchronize(st), "sync");
 }
 
 }  // namespace sq

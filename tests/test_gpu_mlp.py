@@ -124,3 +124,40 @@ def test_learned_start_beats_atomic_superposition(tmp_path):
     m2 = WarmStartMLP(path=path)
     with LSDFT(d, name, faithful=False, precision=32) as eng:
         np.testing.assert_array_equal(m2.predict_density(eng), rho_pred)
+
+
+def test_learned_start_highpass_limits(tmp_path):
+    """sq_scf_options.learned_highpass: the start keeps the network's correction to the
+    superposition scaled by the Kerker symbol k^2/(k^2 + k0^2).  A tiny k0 keeps all of it
+    (the plain learned start, up to the k = 0 mode that the electron count fixes), a huge k0
+    none (the superposition); every start is non-negative with N_e electrons."""
+    import ctypes
+    from sqminiapp_gb300 import LSDFT, WarmStartMLP
+    from sqminiapp_gb300.capi import check
+    from sqminiapp_gb300.decks import make_fcc_mg_deck
+    d, name, meta = make_fcc_mg_deck(str(tmp_path), "c", ncell=1, h=0.85, rcut=3.4, n_qp=20,
+                                     disp=0.25, disp_kind="gaussian", seed=11)
+    rng = np.random.default_rng(12)
+    m = WarmStartMLP(seed=9)
+    m.set_params(_params(rng))
+    with LSDFT(d, name, faithful=False, precision=32) as eng:
+        dV = float(np.prod(eng.info.h[:]))
+
+        def start(k0):
+            opt = eng._scf_options(None, None, None, None, None, None, None,
+                                   learned_highpass=k0)
+            check(eng._lib.sq_scf_begin_learned(eng._h, ctypes.byref(opt), m._m), "learned")
+            return eng.scf_density()[1].copy()
+
+        plain, low, high, mid = start(0.0), start(1e-6), start(1e6), start(1.0)
+        eng.scf_begin()
+        rho0 = eng.scf_density()[1].copy()
+    ne = rho0.sum() * dV
+    for r in (plain, low, high, mid):
+        assert np.all(r >= 0.0)
+        assert r.sum() * dV == pytest.approx(ne, rel=1e-12)
+    scale = np.max(np.abs(plain))
+    assert np.max(np.abs(low - plain)) < 1e-6 * scale
+    assert np.max(np.abs(high - rho0)) < 1e-6 * scale
+    # k0 = 1/bohr keeps part of the correction: strictly between the two
+    assert 0 < np.linalg.norm(mid - rho0) < np.linalg.norm(plain - rho0)
