@@ -154,6 +154,61 @@ __host__ __device__ constexpr int pair_u_planes(int nz, int zsplit) {
   return zsplit > nz - zsplit ? zsplit : nz - zsplit;
 }
 
+// The per-node projector list (records and point indices) is written once per node and read
+// twice per Lanczos step from L2: its stores and loads carry an L2 evict-last cache policy so
+// that other traffic does not push it out between the steps.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+  unsigned long long pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void st_keep(float4 *p, float4 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x),
+               "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void st_keep(unsigned *p, unsigned v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ float4 ld_keep(const float4 *p, unsigned long long pol) {
+  float4 v;
+  asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ unsigned ld_keep(const unsigned *p, unsigned long long pol) {
+  unsigned v;
+  asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+// one list record (N values of chi_lm, zero-padded to whole float4) with the policy above
+template <int N>
+__device__ __forceinline__ void rec_store_keep(float4 *rec, int e, const float *v,
+                                               unsigned long long pol) {
+  constexpr int nv = (N + 3) / 4;
+#pragma unroll
+  for (int j = 0; j < nv; j++) {
+    float t[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) t[q] = 4 * j + q < N ? v[4 * j + q] : 0.f;
+    st_keep(rec + (size_t)e * nv + j, make_float4(t[0], t[1], t[2], t[3]), pol);
+  }
+}
+template <int N>
+__device__ __forceinline__ void rec_load_keep(const float4 *rec, int e, float *c,
+                                              unsigned long long pol) {
+  constexpr int nv = (N + 3) / 4;
+#pragma unroll
+  for (int j = 0; j < nv; j++) {
+    const float4 x = ld_keep(rec + (size_t)e * nv + j, pol);
+    const float t[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (4 * j + q < N) c[4 * j + q] = t[q];
+  }
+}
+
 // PAIR: one node per cluster of two CTAs (the cube split in z, see PairPlanes); else one node
 // per CTA.
 template <int MASK, int MAXT, bool ISO, bool PAIR>
@@ -239,6 +294,8 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
   float4 *P4 = reinterpret_cast<float4 *>(P);
   float4 *U4 = reinterpret_cast<float4 *>(U);
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const unsigned long long kpol = l2_keep_policy();
+  static_assert(std::is_same<typename Rec::vec_t, float4>::value, "FP32 records of float4");
 
   // thread -> quad of a row (pass A) / of a plane (pass B): nq consecutive threads own the
   // quads of one row or plane, so consecutive threads touch consecutive 16-byte quads
@@ -406,8 +463,8 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
           channel(std::integral_constant<int, 2>{});
           channel(std::integral_constant<int, 3>{});
           const int e = pref[kk] + kept_n + __popc(m & ((1u << lane) - 1u));
-          Rec::store(rec, e, out);
-          ridx[e] = (unsigned)(v.pbase + lz * PS + ly * pitch + lx);
+          rec_store_keep<NLM>(rec, e, out, kpol);
+          st_keep(ridx + e, (unsigned)(v.pbase + lz * PS + ly * pitch + lx), kpol);
         }
         kept_n += __popc(m);
       }
@@ -472,8 +529,8 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
 #pragma unroll
             for (int u = 0; u < kStreamG; u++) {
               const int e = min(i0 + 32 * u, kend - 1) + shift;
-              ix[u] = ridx[e];
-              Rec::load(rec, e, c[u]);
+              ix[u] = ld_keep(ridx + e, kpol);
+              rec_load_keep<NLM>(rec, e, c[u], kpol);
             }
 #pragma unroll
             for (int u = 0; u < kStreamG; u++) {
@@ -702,8 +759,8 @@ __device__ __forceinline__ void quad_body(const LanczosParams &p, const float *_
 #pragma unroll
             for (int u = 0; u < kStreamS; u++) {
               const int e = min(i0 + 32 * u, kend - 1) + shift;
-              ix[u] = ridx[e];
-              Rec::load(rec, e, c[u]);
+              ix[u] = ld_keep(ridx + e, kpol);
+              rec_load_keep<NLM>(rec, e, c[u], kpol);
             }
 #pragma unroll
             for (int u = 0; u < kStreamS; u++) {

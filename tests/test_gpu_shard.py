@@ -2,7 +2,9 @@
 with one rank it reproduces the engine's own SCF (SCF_LSSGQ), and with two ranks (two
 handles of the same cell, each doing half the nodes, exchanging on the host through
 ThreadComm; no kernel waits on another) it reproduces the one-rank run.  Free energy per
-atom to 1e-10 Ha over the whole history, same iteration count; FP64 engine."""
+atom to 1e-10 Ha over the whole history and the final Fermi level to 1e-10 Ha, same iteration
+count; FP64 engine.  (Its single-pass kernel sums the projector coefficients with shared
+atomics, so two runs differ in summation order; over an SCF that moves lambda_f by ~1e-11.)"""
 import threading
 
 import numpy as np
@@ -36,7 +38,7 @@ def test_one_rank_matches_engine_scf(small_cell):
     natoms = ref["free_energy"] / ref["free_energy_per_atom"]  # the history holds totals
     np.testing.assert_allclose([h[0] for h in hist], ref["free_energy_history"] / natoms,
                                rtol=0, atol=1e-10)
-    assert abs(hist[-1][2] - ref["lambda_f"]) < 1e-11
+    assert abs(hist[-1][2] - ref["lambda_f"]) < 1e-10
     assert max(rounds) <= 14
 
 
