@@ -473,7 +473,7 @@ def batch_leg(args, local, reps=3):
 
 
 RES_STOP = 3e-5   # relative density residual, the FP32 engine's floor-safe tolerance
-DF_STOP = 1e-5    # |F_k - F_(k-1)| per atom (Ha), the benchmark spec's energy tolerance
+DF_STOP = 1e-5    # |F_k - F_(k-1)| per atom (Ha), the free-energy accuracy target
 
 
 def _scf_trace(eng, mixing, tol, model=None, maxit=100, highpass=0.0):
