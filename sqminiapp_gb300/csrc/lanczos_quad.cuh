@@ -40,6 +40,18 @@
 // head and tail added with error-free transformations, about 48 bits of significand): GB300's
 // FP64 pipe runs at a small fraction of its FP32 rate, so the step loop keeps FP64 out of its
 // critical path and converts to double only to store a_k and b_k.
+//
+// Memory traffic.  In the 12-warp budget pass A reads Veff through a per-thread ring of four
+// float4 in shared memory, filled by cp.async three planes ahead (slot-major: each warp access
+// is 512 contiguous bytes).  The list's stores and loads carry an L2 evict-last policy.  Nodes
+// after the first round come from a device-side queue.
+//
+// CTA pair (PAIR, lanczos_quad_pair_kernel): one node per cluster of two CTAs for cubes whose
+// P and U do not fit one CTA.  The cube is split in z (PairPlanes); each CTA owns its planes of
+// U and of the list and holds P on its planes plus the 6 the z stencil reads from the peer's
+// side, which the peer stores there in its update phase (distributed shared memory).  Barriers
+// 2 and 4 become cluster barriers; c is exchanged per slot after phase 2 and a_k, b_k are
+// summed from both CTAs' partials in rank order, so both CTAs take every branch together.
 #pragma once
 
 #include <cooperative_groups.h>
