@@ -164,3 +164,52 @@ def test_engine_plans_a_pair_for_33_cubes(tmp_path):
     with pytest.raises(Exception):
         plan_kernel(d, name, precision=64)
     assert plan_kernel(d, name, faithful=True).kernel_layout & 32 == 0
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_pair_step_algebra_matches_one_cta(seed):
+    """One Lanczos step split as the pair splits it (FP64 here): each CTA gathers c over the
+    list points of its own planes, a_k = CTA 0's stencil partials + CTA 1's + sum Gamma c^2
+    with c = c_0 + c_1, the scatter adds chi alpha on each CTA's own planes, and b_k^2 sums
+    both CTAs' |w|^2 -- the same a_k, b_k and w as the single-CTA step."""
+    rng = np.random.default_rng(seed)
+    n, nlm = 15, 4
+    zs = (n + 1) // 2
+    N = n ** 3
+    z_of = np.repeat(np.arange(n), n * n)  # point index (z slowest) -> plane
+    own = [z_of < zs, z_of >= zs]
+    # local operator: diagonal plus a 7-point-like banded part in the flattened cube
+    Hl = np.diag(rng.uniform(0.5, 3.0, N))
+    for off in (1, n, n * n):
+        band = rng.uniform(-0.5, 0.0, N - off)
+        Hl += np.diag(band, off) + np.diag(band, -off)
+    m = 3
+    chi = [np.where(rng.random((N, 1)) < 0.2, rng.standard_normal((N, nlm)), 0.0) for _ in range(m)]
+    gam = [rng.uniform(-1.0, 1.0, nlm) for _ in range(m)]
+    P = rng.standard_normal(N)
+    U = rng.standard_normal(N)
+    tb = 1.7
+    inv = 1.0 / tb
+    v = P * inv
+    # single CTA
+    Hv = Hl @ v
+    c = [x.T @ v for x in chi]
+    a1 = v @ Hv + sum(g @ (cc * cc) for g, cc in zip(gam, c))
+    w1 = Hv - tb * U + sum(x @ (g * cc) for x, g, cc in zip(chi, gam, c)) - a1 * v
+    b1 = np.sqrt(w1 @ w1)
+    # the pair
+    cpart = [[x[own[r]].T @ P[own[r]] for x in chi] for r in (0, 1)]   # phase 2 rows
+    cx = [(cpart[0][k] + cpart[1][k]) * inv for k in range(m)]
+    a_loc = [v[own[r]] @ Hv[own[r]] for r in (0, 1)]                     # passes A and B
+    a_nl = sum(g @ (cc * cc) for g, cc in zip(gam, cx))
+    a2 = (a_loc[0] + a_loc[1]) + a_nl
+    w2 = np.empty(N)
+    b2sq = 0.0
+    for r in (0, 1):
+        sel = own[r]
+        Ur = (Hv - tb * U)[sel] + sum(x[sel] @ (g * cc) for x, g, cc in zip(chi, gam, cx))
+        w2[sel] = Ur - a2 * v[sel]
+        b2sq += w2[sel] @ w2[sel]
+    np.testing.assert_allclose(a2, a1, rtol=1e-13)
+    np.testing.assert_allclose(np.sqrt(b2sq), b1, rtol=1e-13)
+    np.testing.assert_allclose(w2, w1, rtol=1e-12, atol=1e-12)
